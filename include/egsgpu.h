@@ -1,0 +1,141 @@
+/*
+ * egsgpu -- C ABI of the GB300 voxel-dose transport engine.
+ *
+ * This is the drop-in boundary for EGSnrc's particle-history loop on the
+ * egs++ EGS_XYZGeometry / DOSXYZnrc path.  Each entry point names the
+ * reference interface it replaces (paths relative to HEN_HOUSE).  Every
+ * function returns an int status (0 = ok, >0 = error class, see
+ * EGSGPU_ERR_*); nothing calls exit().  The library owns all device
+ * buffers; the caller owns every host array passed in (copied on entry).
+ * One handle per host thread; handles are independent.
+ */
+#ifndef EGSGPU_H
+#define EGSGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EGSGPU_OK 0
+#define EGSGPU_ERR_ARG 1       /* bad argument / unsupported option            */
+#define EGSGPU_ERR_DATA 2      /* data file missing or malformed                */
+#define EGSGPU_ERR_MEDIUM 3    /* medium not found / inconsistent PEGS4 block   */
+#define EGSGPU_ERR_CUDA 4      /* CUDA runtime error                            */
+#define EGSGPU_ERR_CAPACITY 5  /* particle queue capacity exceeded              */
+#define EGSGPU_ERR_LOOP 6      /* a device loop hit its iteration cap           */
+#define EGSGPU_ERR_STATE 7     /* call order violated (e.g. run before media)   */
+
+typedef struct egsgpu_handle egsgpu_handle;
+
+/* Transport parameters: the egs++ ":start MC transport parameter:" block
+ * (egs++/egs_advanced_application.cpp:482-562) restricted to the physics
+ * profile this engine implements (PRESTA-II, EXACT BCA, spin off, bound
+ * Compton norej, Rayleigh on, EADL relaxation, Sauter photo-electrons,
+ * BH brems with KM angles, BH pair with simple angles). */
+typedef struct {
+    double ecut;          /* global electron cut-off, total energy (MeV)   */
+    double pcut;          /* global photon cut-off (MeV)                    */
+    double estepe;        /* max fractional energy loss per step (0.25)     */
+    double ximax;         /* max first GS moment per step (0.5)             */
+    double skindepth;     /* skin depth for BCA in elastic MFPs (3)         */
+    int precision;        /* 32: FP32 transport (FP64 tallies); 64: FP64    */
+    int block_size;       /* threads per CTA for the transport kernels; 0 = default */
+    int ctas_per_sm;      /* resident CTAs per SM; 0 = default                       */
+    long long chunk;      /* histories per wavefront chunk; 0 = automatic   */
+    long long capacity;   /* particle-queue capacity per queue; 0 = automatic */
+} egsgpu_config;
+
+/* Source: egs++ EGS_ParallelBeam (sources/egs_parallel_beam) with a point
+ * or rectangle shape (shapes/egs_rectangle) and a monoenergetic or
+ * histogram spectrum (egs_spectra.cpp:491-740). */
+typedef struct {
+    int charge;           /* -1 e-, 0 photon, +1 e+                          */
+    int shape;            /* 0 point, 1 rectangle in the plane z = pos[2]    */
+    double pos[3];        /* point position / plane z                        */
+    double xmin, xmax, ymin, ymax;   /* rectangle extent                     */
+    double dir[3];        /* beam direction (normalised on entry)            */
+    int spectrum;         /* 0 monoenergetic, 1 histogram (counts per MeV)   */
+    double energy;        /* kinetic energy for spectrum 0 (MeV)             */
+    int nbins;            /* spectrum 1: number of bins                       */
+    const double *edges;  /* spectrum 1: nbins+1 bin edges (MeV)              */
+    const double *weights;/* spectrum 1: nbins values, counts per MeV         */
+} egsgpu_source;
+
+/* Default configuration (the egs_set_defaults profile, FP32 transport). */
+void egsgpu_default_config(egsgpu_config *cfg);
+
+/* Creates a handle on the current CUDA device.
+ * Replaces egsInit + egs_set_defaults (interface/egs_interface2.h:712-740,
+ * src/egs_utilities.mortran:896). */
+int egsgpu_create(const egsgpu_config *cfg, egsgpu_handle **out);
+
+/* Reads the PEGS4 blocks of the named media and builds every table
+ * (XCOM photon cross sections, MS surface, Compton shells, photo edges).
+ * Replaces egsAddMedium + egsHatch (interface/egs_interface2.h:760-790;
+ * src/egsnrc.mortran:1828 HATCH). Medium k of `names` is medium index k. */
+int egsgpu_load_media(egsgpu_handle *h, const char *data_dir, const char *pegs_file,
+                      const char *const *names, int n);
+
+/* Voxel phantom: plane positions (nx+1, ny+1, nz+1, cm), medium index and
+ * relative density per voxel, voxel index ix + iy*nx + iz*nx*ny.
+ * Replaces EGS_XYZGeometry construction and the egsHowfar/egsHownear/
+ * egsStartParticle callbacks (egs++/geometry/egs_nd_geometry/egs_nd_geometry.h:769-1379,
+ * egs++/egs_advanced_application.cpp:1351-1442). */
+int egsgpu_set_xyz_geometry(egsgpu_handle *h, int nx, int ny, int nz, const double *xb,
+                            const double *yb, const double *zb, const int32_t *med,
+                            const double *rhor);
+
+/* Replaces EGS_BaseSource::getNextParticle for the parallel-beam source
+ * (egs++/egs_base_source.h:684, sources/egs_parallel_beam/egs_parallel_beam.h:150). */
+int egsgpu_set_source(egsgpu_handle *h, const egsgpu_source *src);
+
+/* Transports histories [first, first+n) in n_batch statistical batches with
+ * Philox streams keyed by (seed, history index); results are independent
+ * of chunking. Accumulates into the handle's tallies (call egsgpu_reset to
+ * clear). `stream` is a cudaStream_t or NULL for the default stream; the
+ * call returns after the work on it has completed.
+ * Replaces EGS_Application::runSimulation / simulateSingleShower / egsShower
+ * (egs++/egs_application.cpp:839-959, interface/egs_interface2.c:92-99). */
+int egsgpu_run(egsgpu_handle *h, long long first, long long n, int n_batch, uint32_t seed,
+               void *stream);
+
+/* Clears tallies and counters. */
+int egsgpu_reset(egsgpu_handle *h);
+
+/* Per-voxel tallies over all batches run so far: sum of batch energy
+ * deposits and sum of their squares (MeV, FP64), plus totals[8] =
+ * {histories, batches, deposited, escaped, steps, photon steps, electron steps, pushes}.
+ * Any pointer may be NULL. Replaces EGS_ScoringArray / DOSXYZ endep,endep2
+ * (egs++/egs_scoring.h:219-390, user_codes/dosxyznrc/dosxyznrc.mortran:1229-1235). */
+int egsgpu_get_tallies(egsgpu_handle *h, double *edep_sum, double *edep2_sum, double *totals);
+
+/* Dose per source particle (Gy) and its 1-sigma uncertainty (Gy) from the
+ * batch tallies: D = E*1.602e-10/(rho*V*N). Replaces
+ * EGS_DoseScoring::reportResults/outputDoseFile
+ * (ausgab_objects/egs_dose_scoring/egs_dose_scoring.cpp:309-480). */
+int egsgpu_get_dose(egsgpu_handle *h, double *dose, double *sigma);
+
+/* Optional per-history deposited energy (MeV) for histories
+ * [first, first+n) of the next egsgpu_run call (n <= 2^24); pass NULL to
+ * disable. A checking aid with no counterpart in the reference API. */
+int egsgpu_set_history_tally(egsgpu_handle *h, long long first, long long n);
+int egsgpu_get_history_tally(egsgpu_handle *h, double *out);
+
+/* Checkpoint / restore of the run state (tallies, counters, next history
+ * index). Replaces the .egsdat output/readData pair
+ * (egs++/egs_application.cpp:482-560). `size` is in/out. */
+int egsgpu_checkpoint(egsgpu_handle *h, void *buf, size_t *size);
+int egsgpu_restore(egsgpu_handle *h, const void *buf, size_t size);
+
+/* Last error message of the handle (never NULL). */
+const char *egsgpu_last_error(egsgpu_handle *h);
+
+void egsgpu_destroy(egsgpu_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EGSGPU_H */

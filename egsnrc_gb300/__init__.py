@@ -1,0 +1,233 @@
+"""egsnrc_gb300: GB300-native coupled photon/electron voxel-dose transport.
+
+Python mirror of the egs++ voxel-dose application path (EGS_XYZGeometry +
+EGS_ParallelBeam + EGS_DoseScoring), driving the CUDA engine through the C
+ABI declared in include/egsgpu.h.  The engine library must be built
+(``python -m egsnrc_gb300.build``); importing the transport classes without
+it raises instead of falling back to anything else.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DATA_DIR = os.path.join(HERE, "data")
+PEGS_FILE = os.path.join(DATA_DIR, "521icru.pegs4dat")
+RM = 0.5109989461
+
+ERRORS = {1: "bad argument", 2: "data file", 3: "medium", 4: "CUDA", 5: "queue capacity",
+          6: "iteration cap", 7: "call order"}
+
+
+class EGSError(RuntimeError):
+    """An engine call returned a non-zero status (the C ABI's error class)."""
+
+    def __init__(self, code, msg):
+        super().__init__("egsgpu error %d (%s): %s" % (code, ERRORS.get(code, "?"), msg))
+        self.code = code
+
+
+class Config(C.Structure):
+    _fields_ = [("ecut", C.c_double), ("pcut", C.c_double), ("estepe", C.c_double), ("ximax", C.c_double),
+                ("skindepth", C.c_double), ("precision", C.c_int), ("block_size", C.c_int),
+                ("ctas_per_sm", C.c_int), ("chunk", C.c_longlong), ("capacity", C.c_longlong)]
+
+
+class SourceStruct(C.Structure):
+    _fields_ = [("charge", C.c_int), ("shape", C.c_int), ("pos", C.c_double * 3), ("xmin", C.c_double),
+                ("xmax", C.c_double), ("ymin", C.c_double), ("ymax", C.c_double), ("dir", C.c_double * 3),
+                ("spectrum", C.c_int), ("energy", C.c_double), ("nbins", C.c_int),
+                ("edges", C.POINTER(C.c_double)), ("weights", C.POINTER(C.c_double))]
+
+
+_LIB = None
+
+
+def library_path():
+    return os.path.join(HERE, "libegsgpu.so")
+
+
+def load_library():
+    """Loads libegsgpu.so (the CUDA engine). Raises if it has not been built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not os.path.exists(path):
+        raise RuntimeError("libegsgpu.so not built: run `python -m egsnrc_gb300.build`")
+    L = C.CDLL(path)
+    vp, i64, dp = C.c_void_p, C.c_longlong, C.POINTER(C.c_double)
+    L.egsgpu_default_config.argtypes = [C.POINTER(Config)]
+    L.egsgpu_create.argtypes = [C.POINTER(Config), C.POINTER(vp)]
+    L.egsgpu_load_media.argtypes = [vp, C.c_char_p, C.c_char_p, C.POINTER(C.c_char_p), C.c_int]
+    L.egsgpu_set_xyz_geometry.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp, dp, dp, C.POINTER(C.c_int32), dp]
+    L.egsgpu_set_source.argtypes = [vp, C.POINTER(SourceStruct)]
+    L.egsgpu_run.argtypes = [vp, i64, i64, C.c_int, C.c_uint32, vp]
+    L.egsgpu_reset.argtypes = [vp]
+    L.egsgpu_get_tallies.argtypes = [vp, dp, dp, dp]
+    L.egsgpu_get_dose.argtypes = [vp, dp, dp]
+    L.egsgpu_set_history_tally.argtypes = [vp, i64, i64]
+    L.egsgpu_get_history_tally.argtypes = [vp, dp]
+    L.egsgpu_checkpoint.argtypes = [vp, vp, C.POINTER(C.c_size_t)]
+    L.egsgpu_restore.argtypes = [vp, vp, C.c_size_t]
+    L.egsgpu_last_error.argtypes = [vp]
+    L.egsgpu_last_error.restype = C.c_char_p
+    L.egsgpu_destroy.argtypes = [vp]
+    _LIB = L
+    return L
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class XYZGeometry:
+    """EGS_XYZGeometry: plane positions (cm), medium index and relative density per voxel
+    (voxel index ix + iy*nx + iz*nx*ny)."""
+
+    def __init__(self, xb, yb, zb, med, rhor=None):
+        self.xb = np.ascontiguousarray(xb, dtype=np.float64)
+        self.yb = np.ascontiguousarray(yb, dtype=np.float64)
+        self.zb = np.ascontiguousarray(zb, dtype=np.float64)
+        self.nx, self.ny, self.nz = len(self.xb) - 1, len(self.yb) - 1, len(self.zb) - 1
+        nv = self.nx * self.ny * self.nz
+        self.med = np.ascontiguousarray(np.broadcast_to(np.asarray(med, dtype=np.int32).ravel(), (nv,)),
+                                        dtype=np.int32)
+        r = np.ones(nv) if rhor is None else np.asarray(rhor, dtype=np.float64).ravel()
+        self.rhor = np.ascontiguousarray(np.broadcast_to(r, (nv,)), dtype=np.float64)
+
+    @staticmethod
+    def uniform(n, size, origin=(0.0, 0.0, 0.0), med=0, rhor=None):
+        nx, ny, nz = (n, n, n) if np.isscalar(n) else n
+        dx, dy, dz = (size, size, size) if np.isscalar(size) else size
+        return XYZGeometry(origin[0] + dx * np.arange(nx + 1), origin[1] + dy * np.arange(ny + 1),
+                           origin[2] + dz * np.arange(nz + 1), med, rhor)
+
+    @property
+    def nvox(self):
+        return self.nx * self.ny * self.nz
+
+    def volumes(self):
+        dx, dy, dz = np.diff(self.xb), np.diff(self.yb), np.diff(self.zb)
+        return (dz[:, None, None] * dy[None, :, None] * dx[None, None, :]).ravel()
+
+
+class ParallelBeam:
+    """EGS_ParallelBeam with a point or rectangle shape and a monoenergetic or
+    histogram spectrum (energies are kinetic, MeV)."""
+
+    def __init__(self, charge=0, energy=None, spectrum=None, position=(0.0, 0.0, 0.0), direction=(0.0, 0.0, 1.0),
+                 rectangle=None):
+        self.s = SourceStruct()
+        self.s.charge = int(charge)
+        self.s.pos[:] = tuple(float(v) for v in position)
+        self.s.dir[:] = tuple(float(v) for v in direction)
+        if rectangle is not None:
+            self.s.shape = 1
+            self.s.xmin, self.s.xmax, self.s.ymin, self.s.ymax = (float(v) for v in rectangle)
+        if spectrum is None:
+            self.s.spectrum = 0
+            self.s.energy = float(energy)
+            self._edges = self._w = None
+        else:
+            edges, weights = spectrum
+            self._edges = np.ascontiguousarray(edges, dtype=np.float64)
+            self._w = np.ascontiguousarray(weights, dtype=np.float64)
+            self.s.spectrum = 1
+            self.s.nbins = len(self._w)
+            self.s.edges = _dp(self._edges)
+            self.s.weights = _dp(self._w)
+            self.s.energy = float(self._edges[-1])
+
+
+def default_config(**kw):
+    cfg = Config()
+    load_library().egsgpu_default_config(C.byref(cfg))
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+class DoseEngine:
+    """One engine handle (egsgpu_create) with its media, phantom, source and tallies."""
+
+    def __init__(self, media, config=None, data_dir=DATA_DIR, pegs_file=PEGS_FILE, **kw):
+        self.L = load_library()
+        self.cfg = config if config is not None else default_config(**kw)
+        h = C.c_void_p()
+        self._check(self.L.egsgpu_create(C.byref(self.cfg), C.byref(h)), None)
+        self.h = h
+        names = (C.c_char_p * len(media))(*[m.encode() for m in media])
+        self.media = list(media)
+        self._check(self.L.egsgpu_load_media(self.h, data_dir.encode(), pegs_file.encode(), names, len(media)))
+        self.geom = None
+
+    def _check(self, rc, h=True):
+        if rc:
+            msg = self.L.egsgpu_last_error(self.h if h else None).decode() if h else "create failed"
+            raise EGSError(rc, msg)
+
+    def set_geometry(self, g):
+        self.geom = g
+        self._check(self.L.egsgpu_set_xyz_geometry(self.h, g.nx, g.ny, g.nz, _dp(g.xb), _dp(g.yb), _dp(g.zb),
+                                                   g.med.ctypes.data_as(C.POINTER(C.c_int32)), _dp(g.rhor)))
+
+    def set_source(self, src):
+        self.src = src
+        self._check(self.L.egsgpu_set_source(self.h, C.byref(src.s)))
+
+    def run(self, n, nbatch=10, seed=1, first=0, stream=None):
+        st = C.c_void_p(stream) if stream else None
+        self._check(self.L.egsgpu_run(self.h, int(first), int(n), int(nbatch), int(seed), st))
+
+    def reset(self):
+        self._check(self.L.egsgpu_reset(self.h))
+
+    def tallies(self):
+        nv = self.geom.nvox
+        s, s2, t = np.zeros(nv), np.zeros(nv), np.zeros(8)
+        self._check(self.L.egsgpu_get_tallies(self.h, _dp(s), _dp(s2), _dp(t)))
+        return s, s2, t
+
+    def totals(self):
+        t = np.zeros(8)
+        self._check(self.L.egsgpu_get_tallies(self.h, None, None, _dp(t)))
+        return dict(histories=t[0], batches=t[1], deposited=t[2], escaped=t[3], steps=t[4], photon_steps=t[5],
+                    electron_steps=t[6], pushes=t[7])
+
+    def dose(self):
+        nv = self.geom.nvox
+        d, s = np.zeros(nv), np.zeros(nv)
+        self._check(self.L.egsgpu_get_dose(self.h, _dp(d), _dp(s)))
+        return d, s
+
+    def set_history_tally(self, first, n):
+        self._hist_n = n
+        self._check(self.L.egsgpu_set_history_tally(self.h, int(first), int(n)))
+
+    def history_tally(self):
+        out = np.zeros(self._hist_n)
+        self._check(self.L.egsgpu_get_history_tally(self.h, _dp(out)))
+        return out
+
+    def checkpoint(self):
+        size = C.c_size_t(0)
+        self._check(self.L.egsgpu_checkpoint(self.h, None, C.byref(size)))
+        buf = C.create_string_buffer(size.value)
+        self._check(self.L.egsgpu_checkpoint(self.h, buf, C.byref(size)))
+        return buf.raw
+
+    def restore(self, blob):
+        self._check(self.L.egsgpu_restore(self.h, blob, len(blob)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.egsgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,156 @@
+// Device-side data layout, random numbers and interaction samplers of the
+// GB300 transport engine.  Templated on the transport precision Real
+// (float or double); tallies are always FP64 and the residual-range /
+// energy-loss arithmetic uses RT (FP64 in both precisions).
+// Paths in comments are relative to the EGSnrc HEN_HOUSE directory.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace egsgpu {
+
+constexpr double RM = 0.5109989461;   // src/egsnrc.macros:1140
+constexpr int MXGE = 2000;
+constexpr int NRAY = 100;
+constexpr int MS_NL = 64, MS_NQ = 8, MS_NU = 32;
+constexpr int MAXMED = 16;            // media per problem (constant-memory scalars)
+constexpr int MAXNE = 12;             // elements per medium
+constexpr int LOOP_CAP = 100000;      // cap on every rejection loop
+typedef double RT;                    // residual range / energy loss type
+
+// ------------------------------------------------------------- tables ----
+// Per-medium scalars, one struct per medium in constant memory.
+template <class Real>
+struct MedScalars {
+    Real rho, ae, ap, te, thmoll, blcc, xcc, eke0, eke1, ge0, ge1, esig_e, psig_e, log_ap, delcm,
+        zbrang, lzbrang;
+    Real dl[6][8];
+    Real bpar[2];
+    RT E_array0;
+    int meke, n_shell, nne, sig_mono_e, sig_mono_p;
+    int etab_off, gtab_off, shell_off, elem_off;
+    float pz[MAXNE];
+};
+
+// Device pointers into the table blob.
+template <class Real>
+struct Tables {
+    const Real *etab;     // [medium][meke][16]: esig0,esig1,psig0,psig1,ededx0,ededx1,pdedx0,pdedx1,
+                          //                     ebr10,ebr11,pbr10,pbr11,pbr20,pbr21,tmxs0,tmxs1
+    const RT *erange;     // [medium][meke][4]: E_array, range_ep0, range_ep1, pad
+    const Real *gtab;     // [medium][MXGE][8]: gmfp0,gmfp1,gbr10,gbr11,gbr20,gbr21,cohe0,cohe1
+    const Real *pmax;     // [medium][MXGE][2]
+    const Real *ray;      // [medium][4][NRAY]: xgrid, fcum, b_array, c_array
+    const int *ray_i;     // [medium][NRAY] (1-based bins)
+    const Real *shell;    // [shell_off + i][4]: eno (alias threshold), be (rm units), Jo, erfJo
+    const int *shell_at;  // [shell_off + i]: alias bin (1-based)
+    const Real *elem;     // [elem_off + k][96]: edge_a[16] b[16] c[16] d[16] energies[16] binding[6] iprob[6] | nedge
+    const Real *ms;       // [MS_NL*MS_NQ*MS_NU][3]: ums, fms, wms
+    const int *ms_i;      // [MS_NL*MS_NQ*MS_NU]
+    Real dllambi, dqmsi;
+    int nmed;
+    // run parameters
+    Real ecut, pcut, skindepth, smaxir;
+};
+
+// ------------------------------------------------------------ geometry ----
+template <class Real>
+struct Geom {
+    int nx, ny, nz, nxy;
+    const Real *xb, *yb, *zb;
+    const uint8_t *med;
+    const Real *rhor;
+    Real bt, hbt;         // boundary tolerance (egs++/egs_functions.h:80-88)
+};
+
+// ------------------------------------------------------------- source ----
+struct Source {
+    int charge, shape, spectrum, nbins;
+    double pos[3], xmin, xmax, ymin, ymax, dir[3], energy;
+    const double *edges;  // device
+    const double *wi;     // device alias weights
+    const int *bin;       // device alias bins
+};
+
+// -------------------------------------------------------------- queues ----
+// Structure-of-arrays particle queue in HBM.  Photon queues ignore iq.
+template <class Real>
+struct Queue {
+    Real *x, *y, *z, *u, *v, *w, *E, *wt;
+    int *ir;
+    int8_t *iq;
+    uint32_t *hist, *n;
+    unsigned long long *sid;
+    unsigned int *count;  // device counter (pushes)
+    unsigned int capacity;
+};
+
+// ---------------------------------------------------------------- RNG ----
+// Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) keyed by (seed, history)
+// with counter (block, stream id lo, stream id hi, 0).
+__host__ __device__ inline void philox10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
+                                         uint32_t k1, uint32_t out[4]) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+#ifdef __CUDA_ARCH__
+        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+#else
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0, hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+#endif
+        uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+__host__ __device__ inline uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__host__ __device__ inline uint64_t child_sid(uint64_t sid, uint32_t n, uint32_t k) {
+    return mix64(sid + 0x9E3779B97F4A7C15ull * (1 + (((uint64_t)n) << 3) + k));
+}
+
+struct Rng {
+    uint32_t seed, hist, n, blk;
+    uint64_t sid;
+    uint32_t c0, c1, c2, c3;
+    __device__ void init(uint32_t s, uint32_t h, uint64_t id, uint32_t n0) {
+        seed = s; hist = h; sid = id; n = n0; blk = 0xffffffffu;
+    }
+    __device__ float u() {
+        uint32_t b = n >> 2;
+        if (b != blk) {
+            uint32_t o[4];
+            philox10(b, (uint32_t)sid, (uint32_t)(sid >> 32), 0u, seed, hist, o);
+            c0 = o[0]; c1 = o[1]; c2 = o[2]; c3 = o[3];
+            blk = b;
+        }
+        uint32_t j = n & 3u, x = (j == 0) ? c0 : (j == 1) ? c1 : (j == 2) ? c2 : c3;
+        ++n;
+        // (x >> 9) + 0.5 scaled by 2^-23: exact in FP32 and FP64, in (0,1)
+        return ((float)(x >> 9) + 0.5f) * (1.0f / 8388608.0f);
+    }
+};
+// Uniform in (0,1) with 23 random bits: the same value in FP32 and FP64.
+template <class Real>
+__device__ inline Real urand(Rng &r) { return (Real)r.u(); }
+
+// --------------------------------------------------------- math shims ----
+__device__ inline float dlog(float x) { return logf(x); }
+__device__ inline double dlog(double x) { return log(x); }
+__device__ inline float dexp(float x) { return expf(x); }
+__device__ inline double dexp(double x) { return exp(x); }
+__device__ inline float dsqrt(float x) { return sqrtf(x); }
+__device__ inline double dsqrt(double x) { return sqrt(x); }
+__device__ inline float dcos(float x) { return cosf(x); }
+__device__ inline double dcos(double x) { return cos(x); }
+template <class T> __device__ inline T dmin(T a, T b) { return a < b ? a : b; }
+template <class T> __device__ inline T dmax(T a, T b) { return a > b ? a : b; }
+template <class T> __device__ inline T dabs(T a) { return a < 0 ? -a : a; }
+
+}  // namespace egsgpu

@@ -1,0 +1,1532 @@
+// GB300 transport kernels and the C-ABI engine behind include/egsgpu.h.
+//
+// Histories run as a wavefront over per-type SoA particle queues in HBM:
+//   k_source    one thread per history: samples the source particle and
+//               places it on the phantom surface (egs++ simulateSingleShower,
+//               egs_application.cpp:919-959, egs_nd_geometry.h:1281-1379)
+//   k_photon    persistent warps; each iteration moves one photon through one
+//               voxel (or to its interaction) and samples the interaction
+//               (PHOTON, src/egsnrc.mortran:6439-6641); electrons are pushed
+//               to the electron queue
+//   k_electron  persistent warps; each iteration takes one condensed-history
+//               step (ELECTR, src/egsnrc.mortran:985-1821) and, when the
+//               sub-threshold energy-loss budget is used up, the discrete
+//               interaction; photons go to the next photon queue, delta rays
+//               to the next electron queue
+//   k_batch     folds the batch tally into the per-voxel sum and sum of squares
+// Energy deposits are accumulated per thread while a particle stays in one
+// voxel and flushed with one FP64 atomic (tallies are L2-resident).
+// Paths in comments are relative to the EGSnrc HEN_HOUSE directory.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/egsgpu.h"
+#include "egs_device.cuh"
+#include "egs_hatch.h"
+#include "egs_physics.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace egsgpu {
+
+__constant__ MedScalars<float> c_med_f[MAXMED];
+__constant__ MedScalars<double> c_med_d[MAXMED];
+template <class Real> __device__ inline const MedScalars<Real> &cmed(int m);
+template <> __device__ inline const MedScalars<float> &cmed<float>(int m) { return c_med_f[m]; }
+template <> __device__ inline const MedScalars<double> &cmed<double>(int m) { return c_med_d[m]; }
+
+// Counters: 0 photon steps, 1 electron steps, 2 pushes, 3 interactions
+// A particle that needs more iterations than this is retired and reported
+// (EGSGPU_ERR_LOOP); no physical history comes near it.
+constexpr int STEP_CAP = 1 << 22;
+
+enum { CNT_PSTEP = 0, CNT_ESTEP = 1, CNT_PUSH = 2, CNT_INTER = 3, CNT_N = 8 };
+
+template <class Real>
+struct Params {
+    Tables<Real> T;
+    Geom<Real> G;
+    Queue<Real> pin, ein, pout, eout;    // consumed / produced queues
+    double *dose;                         // batch tally per voxel
+    double *hist_tally;                   // optional per-history deposits
+    long long hist_first, hist_n;
+    double *energy;                       // [0] deposited, [1] escaped
+    unsigned long long *counters;         // CNT_*
+    int *error;                           // [0] capacity, [1] loop cap
+    uint32_t seed;
+};
+
+// ------------------------------------------------------------- tallies ----
+struct Acc {
+    int ir;
+    uint32_t hist;
+    double e;
+};
+
+template <class Real>
+__device__ inline void acc_flush(const Params<Real> &P, Acc &a) {
+    if (a.ir >= 0 && a.e > 0) {
+        atomicAdd(P.dose + a.ir, a.e);
+        if (P.hist_tally) {
+            long long i = (long long)a.hist - P.hist_first;
+            if (i >= 0 && i < P.hist_n) atomicAdd(P.hist_tally + i, a.e);
+        }
+    }
+    a.e = 0;
+    a.ir = -1;
+}
+template <class Real>
+__device__ inline void deposit(const Params<Real> &P, Acc &a, int ir, uint32_t hist, double e) {
+    if (ir < 0 || !(e > 0)) return;
+    if (ir != a.ir || hist != a.hist) {
+        acc_flush(P, a);
+        a.ir = ir;
+        a.hist = hist;
+    }
+    a.e += e;
+}
+
+// ------------------------------------------------------------- queues ----
+template <class Real>
+__device__ inline void q_store(const Queue<Real> &q, unsigned i, const Particle<Real> &p) {
+    q.x[i] = p.x; q.y[i] = p.y; q.z[i] = p.z;
+    q.u[i] = p.u; q.v[i] = p.v; q.w[i] = p.w;
+    q.E[i] = p.E; q.wt[i] = p.wt; q.ir[i] = p.ir;
+    if (q.iq) q.iq[i] = (int8_t)p.iq;
+    q.hist[i] = p.rng.hist; q.n[i] = p.rng.n; q.sid[i] = p.rng.sid;
+}
+template <class Real>
+__device__ inline void q_load(const Queue<Real> &q, unsigned i, uint32_t seed, Particle<Real> &p) {
+    p.x = q.x[i]; p.y = q.y[i]; p.z = q.z[i];
+    p.u = q.u[i]; p.v = q.v[i]; p.w = q.w[i];
+    p.E = q.E[i]; p.wt = q.wt[i]; p.ir = q.ir[i];
+    p.iq = q.iq ? (int)q.iq[i] : 0;
+    p.rng.init(seed, q.hist[i], q.sid[i], q.n[i]);
+}
+// Warp-aggregated append: the lanes that reach the push together share one
+// atomic on the queue counter.
+template <class Real>
+__device__ inline void q_push(const Params<Real> &P, const Queue<Real> &q, const Particle<Real> &p,
+                              unsigned long long &npush) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    unsigned base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(q.count, (unsigned)g.size());
+    base = g.shfl(base, 0);
+    unsigned i = base + g.thread_rank();
+    if (i < q.capacity) {
+        q_store(q, i, p);
+        ++npush;
+    } else {
+        atomicExch(P.error + 0, 1);
+    }
+}
+
+// ----------------------------------------------------------- geometry ----
+// EGS_XYZGeometry::howfar (egs++/geometry/egs_nd_geometry/egs_nd_geometry.h:963-1104)
+template <class Real>
+__device__ inline int howfar(const Geom<Real> &G, int ireg, Real x, Real y, Real z, Real u, Real v, Real w,
+                             Real &t) {
+    int iz = ireg / G.nxy, ir = ireg - iz * G.nxy, iy = ir / G.nx, ix = ir - iy * G.nx;
+    int inew = ireg;
+    if (u > 0) {
+        Real d = (G.xb[ix + 1] - x) / u;
+        if (d <= t) { t = (d <= G.bt) ? G.hbt : d; inew = (ix + 1 < G.nx) ? ireg + 1 : -1; }
+    } else if (u < 0) {
+        Real d = (G.xb[ix] - x) / u;
+        if (d <= t) { t = (d <= G.bt) ? G.hbt : d; inew = (ix - 1 >= 0) ? ireg - 1 : -1; }
+    }
+    if (v > 0) {
+        Real d = (G.yb[iy + 1] - y) / v;
+        if (d <= t) { t = (d <= G.bt) ? G.hbt : d; inew = (iy + 1 < G.ny) ? ireg + G.nx : -1; }
+    } else if (v < 0) {
+        Real d = (G.yb[iy] - y) / v;
+        if (d <= t) { t = (d <= G.bt) ? G.hbt : d; inew = (iy - 1 >= 0) ? ireg - G.nx : -1; }
+    }
+    if (w > 0) {
+        Real d = (G.zb[iz + 1] - z) / w;
+        if (d <= t) { t = (d <= G.bt) ? G.hbt : d; inew = (iz + 1 < G.nz) ? ireg + G.nxy : -1; }
+    } else if (w < 0) {
+        Real d = (G.zb[iz] - z) / w;
+        if (d <= t) { t = (d <= G.bt) ? G.hbt : d; inew = (iz - 1 >= 0) ? ireg - G.nxy : -1; }
+    }
+    return inew;
+}
+// EGS_XYZGeometry::hownear (egs_nd_geometry.h:1106-1122)
+template <class Real>
+__device__ inline Real hownear(const Geom<Real> &G, int ireg, Real x, Real y, Real z) {
+    int iz = ireg / G.nxy, ir = ireg - iz * G.nxy, iy = ir / G.nx, ix = ir - iy * G.nx;
+    Real t = dmin(x - G.xb[ix], G.xb[ix + 1] - x);
+    t = dmin(t, dmin(y - G.yb[iy], G.yb[iy + 1] - y));
+    t = dmin(t, dmin(z - G.zb[iz], G.zb[iz + 1] - z));
+    return t;
+}
+template <class Real>
+__device__ inline int plane_where(const Real *b, int n, Real x) {
+    if (x < b[0] || x > b[n]) return -1;
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (x < b[mid]) hi = mid; else lo = mid;
+    }
+    return lo;
+}
+
+// ------------------------------------------------------------- source ----
+template <class Real>
+__global__ void k_source(Params<Real> P, Source S, long long first, long long n) {
+    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    uint32_t hist = (uint32_t)(first + t);
+    Particle<Real> p;
+    p.rng.init(P.seed, hist, 0ull, 0u);
+    p.wt = 1;
+    double x = S.pos[0], y = S.pos[1], z = S.pos[2];
+    if (S.shape == 1) {
+        x = S.xmin + (S.xmax - S.xmin) * (double)urand<Real>(p.rng);
+        y = S.ymin + (S.ymax - S.ymin) * (double)urand<Real>(p.rng);
+    }
+    double ek;
+    if (S.spectrum == 0) ek = S.energy;
+    else {
+        double aj = (double)urand<Real>(p.rng) * S.nbins;
+        int j = (int)aj;
+        aj -= j;
+        if (aj > S.wi[j]) j = S.bin[j];
+        ek = S.edges[j] + (S.edges[j + 1] - S.edges[j]) * (double)urand<Real>(p.rng);
+    }
+    p.iq = S.charge;
+    p.E = (Real)(p.iq == 0 ? ek : ek + RM);
+    double u = S.dir[0], v = S.dir[1], w = S.dir[2];
+    const Geom<Real> &G = P.G;
+    // isWhere, then howfarFromOut (egs_nd_geometry.h:1281-1379), in FP64
+    int ix = plane_where(G.xb, G.nx, (Real)x), iy = plane_where(G.yb, G.ny, (Real)y), iz = plane_where(G.zb, G.nz, (Real)z);
+    int ir = (ix >= 0 && iy >= 0 && iz >= 0) ? ix + iy * G.nx + iz * G.nxy : -1;
+    if (ir < 0) {
+        const Real *pl[3] = {G.xb, G.yb, G.zb};
+        int nn[3] = {G.nx, G.ny, G.nz};
+        double pos[3] = {x, y, z}, dir[3] = {u, v, w};
+        for (int a = 0; a < 3 && ir < 0; ++a) {
+            int i = -1;
+            double t1 = 0, b0 = (double)pl[a][0], bn = (double)pl[a][nn[a]];
+            if (pos[a] <= b0 && dir[a] > 0) { t1 = (b0 - pos[a]) / dir[a]; i = 0; }
+            else if (pos[a] >= bn && dir[a] < 0) { t1 = (bn - pos[a]) / dir[a]; i = nn[a] - 1; }
+            if (i < 0 || t1 > 1e10) continue;
+            double q[3] = {pos[0] + dir[0] * t1, pos[1] + dir[1] * t1, pos[2] + dir[2] * t1};
+            int idx[3];
+            bool ok = true;
+            for (int c = 0; c < 3; ++c) {
+                if (c == a) { idx[c] = i; continue; }
+                idx[c] = plane_where(pl[c], nn[c], (Real)q[c]);
+                if (idx[c] < 0) { ok = false; break; }
+            }
+            if (!ok) continue;
+            int inew = idx[0] + idx[1] * G.nx + idx[2] * G.nxy;
+            if (t1 < (double)G.bt) {
+                Real tt = (Real)t1;
+                int itest = howfar(G, inew, (Real)q[0], (Real)q[1], (Real)q[2], (Real)u, (Real)v, (Real)w, tt);
+                if (itest == -1 && tt < G.bt) break;
+            }
+            x = q[0]; y = q[1]; z = q[2];
+            ir = inew;
+        }
+    }
+    if (ir < 0) return;
+    p.x = (Real)x; p.y = (Real)y; p.z = (Real)z;
+    p.u = (Real)u; p.v = (Real)v; p.w = (Real)w;
+    p.ir = ir;
+    unsigned long long np = 0;
+    if (p.iq == 0) q_push(P, P.pout, p, np);
+    else q_push(P, P.eout, p, np);
+}
+
+// ------------------------------------------------------------- photon ----
+template <class Real>
+struct PhotonState {
+    int state;            // 0 new energy, 1 new medium, 2 transport
+    int medium, nsteps;
+    Real rhor, gle, dpmfp, gmfpr0, cohfac;
+    int lgle;
+};
+
+template <class Real>
+__global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
+    const Tables<Real> &T = P.T;
+    const Geom<Real> &G = P.G;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned nq = *P.pin.count < P.pin.capacity ? *P.pin.count : P.pin.capacity;
+    __shared__ unsigned s_dummy;
+    (void)s_dummy;
+    Particle<Real> p;
+    PhotonState<Real> s;
+    Acc acc{-1, 0u, 0.0};
+    bool alive = false, exhausted = false;
+    unsigned long long nstep = 0, npush = 0, ninter = 0;
+    double edep_tot = 0, esc_tot = 0;
+    int err = 0;
+    const Real rm = (Real)RM;
+    while (true) {
+        unsigned need = __ballot_sync(0xffffffffu, !alive);
+        if (need && !exhausted) {
+            unsigned base = 0;
+            if (lane == (unsigned)(__ffs(need) - 1)) base = atomicAdd(P.pin.count + 1, (unsigned)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, __ffs(need) - 1);
+            if (base >= nq) exhausted = true;
+            if (!alive) {
+                unsigned idx = base + __popc(need & ((1u << lane) - 1u));
+                if (idx < nq) {
+                    q_load(P.pin, idx, P.seed, p);
+                    alive = true;
+                    s.state = 0;
+                    s.nsteps = 0;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, alive)) break;
+        if (!alive) continue;
+
+        if (s.state == 0) {   // :PNEWENERGY:
+            if (p.E <= T.pcut) {   // :PCUT-DISCARD:
+                deposit(P, acc, p.ir, p.rng.hist, (double)(p.E * p.wt));
+                edep_tot += (double)(p.E * p.wt);
+                alive = false;
+                continue;
+            }
+            s.medium = G.med[p.ir];
+            s.rhor = G.rhor[p.ir];
+            s.gle = dlog(p.E);
+            Real r35 = urand<Real>(p.rng);
+            s.dpmfp = -dlog(r35);
+            s.state = 1;
+        }
+        if (s.state == 1) {   // :PNEWMEDIUM:
+            const MedScalars<Real> &M = cmed<Real>(s.medium);
+            s.lgle = min(max((int)(M.ge1 * s.gle + M.ge0), 1), MXGE);
+            const Real *g = T.gtab + ((size_t)M.gtab_off + s.lgle - 1) * 8;
+            s.gmfpr0 = g[1] * s.gle + g[0];
+            s.cohfac = g[7] * s.gle + g[6];
+            s.state = 2;
+        }
+        // :PTRANS: one voxel
+        if (++s.nsteps > STEP_CAP) { err = 1; alive = false; continue; }
+        Real gmfp = s.gmfpr0 / s.rhor * s.cohfac;
+        Real ustep = gmfp * s.dpmfp;
+        int irnew = howfar(G, p.ir, p.x, p.y, p.z, p.u, p.v, p.w, ustep);
+        ++nstep;
+        p.x += p.u * ustep; p.y += p.v * ustep; p.z += p.w * ustep;
+        s.dpmfp = dmax((Real)0, s.dpmfp - ustep / gmfp);
+        if (irnew != p.ir) {
+            p.ir = irnew;
+            if (irnew < 0) { esc_tot += (double)(p.E * p.wt); alive = false; continue; }
+            int mnew = G.med[irnew];
+            s.rhor = G.rhor[irnew];
+            if (mnew != s.medium) { s.medium = mnew; s.state = 1; continue; }
+        }
+        if (s.dpmfp > (Real)1e-8) continue;
+
+        // interaction
+        ++ninter;
+        const MedScalars<Real> &M = cmed<Real>(s.medium);
+        const Real *g = T.gtab + ((size_t)M.gtab_off + s.lgle - 1) * 8;
+        Real r37 = urand<Real>(p.rng);
+        if (r37 <= 1 - s.cohfac) {   // Rayleigh (src/egsnrc.macros:1602-1613)
+            Real costhe, sinthe;
+            rayleigh(T, s.medium, p.E, s.gle, s.lgle, p.rng, costhe, sinthe, err);
+            Azim<Real> az = azimuth<Real>(p.rng, err);
+            Real a = p.u, b = p.v, c = p.w;
+            rotate(a, b, c, sinthe, costhe, az, p.u, p.v, p.w);
+            s.state = 0;
+            continue;
+        }
+        Real r36 = urand<Real>(p.rng);
+        Real gbr1 = g[3] * s.gle + g[2];
+        if (r36 <= gbr1 && p.E > 2 * rm) {
+            Real E2, u2, v2, w2;
+            int iq2;
+            pair(M, p, E2, iq2, u2, v2, w2, err);
+            Particle<Real> q = p;
+            q.E = E2; q.iq = iq2; q.u = u2; q.v = v2; q.w = w2;
+            q.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
+            q_push(P, P.ein, p, npush);
+            q_push(P, P.ein, q, npush);
+            alive = false;
+            continue;
+        }
+        Real gbr2 = g[5] * s.gle + g[4];
+        if (r36 < gbr2) {
+            Particle<Real> e = p;
+            Real edep = compton(T, M, p, e.u, e.v, e.w, e.E, err);
+            e.iq = -1;
+            e.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
+            if (edep > 0) { deposit(P, acc, p.ir, p.rng.hist, (double)(edep * p.wt)); edep_tot += (double)(edep * p.wt); }
+            q_push(P, P.ein, e, npush);
+            s.state = 0;
+            continue;
+        }
+        Real edep = photo(T, M, p, s.gle, err);
+        if (edep > 0) { deposit(P, acc, p.ir, p.rng.hist, (double)(edep * p.wt)); edep_tot += (double)(edep * p.wt); }
+        q_push(P, P.ein, p, npush);
+        alive = false;
+    }
+    acc_flush(P, acc);
+    // block-level counter reduction via warp shuffles
+    for (int o = 16; o > 0; o >>= 1) {
+        nstep += __shfl_down_sync(0xffffffffu, nstep, o);
+        npush += __shfl_down_sync(0xffffffffu, npush, o);
+        ninter += __shfl_down_sync(0xffffffffu, ninter, o);
+        edep_tot += __shfl_down_sync(0xffffffffu, edep_tot, o);
+        esc_tot += __shfl_down_sync(0xffffffffu, esc_tot, o);
+    }
+    if (lane == 0) {
+        atomicAdd(P.counters + CNT_PSTEP, nstep);
+        atomicAdd(P.counters + CNT_PUSH, npush);
+        atomicAdd(P.counters + CNT_INTER, ninter);
+        atomicAdd(P.energy + 0, edep_tot);
+        atomicAdd(P.energy + 1, esc_tot);
+    }
+    if (err) atomicExch(P.error + 1, 1);
+}
+
+// ----------------------------------------------------------- electron ----
+template <class Real>
+struct ElecState {
+    int state;            // 0 new electron, 1 new tstep, 2 ustep
+    int medium, lelke, compute_tstep, nsteps;
+    Real rhor, eke, elke, sig0, demfp;
+    RT total_de, total_tstep;
+};
+
+// Electron-table row accessor: 16 coefficients per energy bin.
+template <class Real>
+struct ERow {
+    const Real *r;
+    int qel;
+    __device__ Real sig(Real elke) const { return qel ? r[3] * elke + r[2] : r[1] * elke + r[0]; }
+    __device__ Real dedx(Real elke) const { return qel ? r[7] * elke + r[6] : r[5] * elke + r[4]; }
+    __device__ Real dedx1() const { return qel ? r[7] : r[5]; }
+};
+
+template <class Real>
+__device__ inline const Real *erow(const Tables<Real> &T, const MedScalars<Real> &M, int lel) {
+    return T.etab + ((size_t)M.etab_off + lel - 1) * 16;
+}
+template <class Real>
+__device__ inline const RT *rrow(const Tables<Real> &T, const MedScalars<Real> &M, int lel) {
+    return T.erange + ((size_t)M.etab_off + lel - 1) * 4;
+}
+
+// $COMPUTE-DRANGE (src/egsnrc.macros:3214-3238)
+template <class Real>
+__device__ inline RT drange(const Tables<Real> &T, const MedScalars<Real> &M, int qel, RT e1, RT e2, int lel,
+                            RT el1, RT el2) {
+    const Real *r = erow(T, M, lel);
+    RT fedep = 1 - e2 / e1;
+    RT elktmp = 0.5 * (el1 + el2 + 0.25 * fedep * fedep * (1 + fedep * (1 + 0.875 * fedep)));
+    RT d0 = qel ? (RT)r[6] : (RT)r[4], d1 = qel ? (RT)r[7] : (RT)r[5];
+    RT dedxmid = 1 / (d1 * elktmp + d0);
+    RT aux = d1 * dedxmid;
+    aux = aux * (1 + 2 * aux) * (fedep / (2 - fedep)) * (fedep / (2 - fedep)) / 6;
+    return fedep * e1 * dedxmid * (1 + aux);
+}
+// $COMPUTE-ELOSS (:3290-3312)
+template <class Real>
+__device__ inline RT eloss(const Tables<Real> &T, const MedScalars<Real> &M, int qel, RT step, RT eke, RT elke,
+                           int lel, RT rhof) {
+    const Real *r = erow(T, M, lel);
+    RT d0 = qel ? (RT)r[6] : (RT)r[4], d1 = qel ? (RT)r[7] : (RT)r[5];
+    RT dedxmid = d1 * elke + d0;
+    RT aux = d1 / dedxmid;
+    RT de = dedxmid * step * rhof;
+    RT fedep = de / eke;
+    return de * (1 - 0.5 * fedep * aux * (1 - 0.333333 * fedep * (aux - 1 - 0.25 * fedep * (2 - aux * (4 - aux)))));
+}
+// $COMPUTE-ELOSS-G (:3315-3351)
+template <class Real>
+__device__ inline RT eloss_g(const Tables<Real> &T, const MedScalars<Real> &M, int qel, RT step, RT eke, RT elke,
+                             int lel, RT range, RT rhof) {
+    RT tuss = range - rrow(T, M, lel)[1 + qel] / rhof;
+    if (tuss >= step) return eloss(T, M, qel, step, eke, elke, lel, rhof);
+    int lt = lel;
+    tuss = (range - step) * rhof;
+    if (tuss <= 0) return eke - (RT)M.te * 0.99;
+    while (lt > 1 && tuss < rrow(T, M, lt)[1 + qel]) --lt;
+    if (lt > M.meke - 1) lt = M.meke - 1;
+    RT elktmp = (lt + 1 - (RT)M.eke0) / (RT)M.eke1, eketmp = rrow(T, M, lt + 1)[0];
+    tuss = (rrow(T, M, lt + 1)[1 + qel] - tuss) / rhof;
+    RT de = eloss(T, M, qel, tuss, eketmp, elktmp, lt, rhof);
+    return de + eke - eketmp;
+}
+
+template <class Real>
+__global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
+    const Tables<Real> &T = P.T;
+    const Geom<Real> &G = P.G;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned nq = *P.ein.count < P.ein.capacity ? *P.ein.count : P.ein.capacity;
+    Particle<Real> p;
+    ElecState<Real> s;
+    Acc acc{-1, 0u, 0.0};
+    bool alive = false, exhausted = false;
+    unsigned long long nstep = 0, npush = 0, ninter = 0;
+    double edep_tot = 0, esc_tot = 0;
+    int err = 0;
+    const Real rm = (Real)RM;
+    while (true) {
+        unsigned need = __ballot_sync(0xffffffffu, !alive);
+        if (need && !exhausted) {
+            unsigned base = 0;
+            if (lane == (unsigned)(__ffs(need) - 1)) base = atomicAdd(P.ein.count + 1, (unsigned)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, __ffs(need) - 1);
+            if (base >= nq) exhausted = true;
+            if (!alive) {
+                unsigned idx = base + __popc(need & ((1u << lane) - 1u));
+                if (idx < nq) {
+                    q_load(P.ein, idx, P.seed, p);
+                    alive = true;
+                    s.state = 0;
+                    s.nsteps = 0;
+                    s.medium = G.med[p.ir];
+                    s.rhor = G.rhor[p.ir];
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, alive)) break;
+        if (!alive) continue;
+
+        const int qel = (1 + p.iq) / 2;
+        bool ecut_discard = false;
+        if (++s.nsteps > STEP_CAP) { err = 1; alive = false; continue; }
+        if (s.state == 0) {   // :NEWELECTRON:
+            if (p.E <= T.ecut) ecut_discard = true;
+            else s.state = 1;
+        }
+        if (!ecut_discard) {
+            if (s.state == 1) {   // :TSTEP:
+                const MedScalars<Real> &M = cmed<Real>(s.medium);
+                s.compute_tstep = 1;
+                s.eke = p.E - rm;
+                Real r = urand<Real>(p.rng);
+                s.demfp = dmax(-dlog(r), (Real)1e-8);
+                s.elke = dlog(s.eke);
+                s.lelke = min(max((int)(M.eke1 * s.elke + M.eke0), 1), M.meke);
+                ERow<Real> er{erow(T, M, s.lelke), qel};
+                if (qel ? M.sig_mono_p : M.sig_mono_e) s.sig0 = er.sig(s.elke) / er.dedx(s.elke);
+                else s.sig0 = qel ? M.psig_e : M.esig_e;
+                s.state = 2;
+            }
+            // :USTEP: one condensed-history step
+            const MedScalars<Real> &M = cmed<Real>(s.medium);
+            Real rhof = s.rhor, sig = s.sig0;
+            RT tstep;
+            const RT *rr = rrow(T, M, s.lelke);
+            if (sig <= 0) { tstep = 1e8; s.sig0 = (Real)1e-15; }
+            else {
+                if (s.compute_tstep) {
+                    s.total_de = (RT)s.demfp / (RT)sig;
+                    RT eke = s.eke, elke = s.elke, ekef = eke - s.total_de;
+                    if (ekef <= M.E_array0) tstep = 1e8;
+                    else {
+                        RT elkef = log(ekef);
+                        int lelkef = min(max((int)((RT)M.eke1 * elkef + (RT)M.eke0), 1), s.lelke);
+                        if (lelkef == s.lelke) tstep = drange(T, M, qel, eke, ekef, s.lelke, elke, elkef);
+                        else {
+                            RT ekei = rr[0], elkei = (s.lelke - (RT)M.eke0) / (RT)M.eke1;
+                            RT tuss = drange(T, M, qel, eke, ekei, s.lelke, elke, elkei);
+                            const RT *rf = rrow(T, M, lelkef + 1);
+                            ekei = rf[0];
+                            elkei = (lelkef + 1 - (RT)M.eke0) / (RT)M.eke1;
+                            tstep = drange(T, M, qel, ekei, ekef, lelkef, elkei, elkef);
+                            tstep = tstep + tuss + rr[1 + qel] - rf[1 + qel];
+                        }
+                    }
+                    s.total_tstep = tstep;
+                    s.compute_tstep = 0;
+                }
+                tstep = s.total_tstep / (RT)rhof;
+            }
+            ERow<Real> er{erow(T, M, s.lelke), qel};
+            const Real *row = er.r;
+            Real dedx0 = er.dedx(s.elke), dedx = rhof * dedx0;
+            Real tmxs = (row[15] * s.elke + row[14]) / rhof;
+            RT range;
+            {
+                RT ekei = rr[0], elkei = (s.lelke - (RT)M.eke0) / (RT)M.eke1;
+                range = drange(T, M, qel, (RT)s.eke, ekei, s.lelke, (RT)s.elke, elkei);
+                range = (range + rr[1 + qel]) / (RT)rhof;
+            }
+            tmxs = dmin(tmxs, T.smaxir);
+            Real tustep = (Real)dmin(tstep, dmin((RT)tmxs, range));
+            Real tperp = hownear(G, p.ir, p.x, p.y, p.z);
+            Real blccl = rhof * M.blcc;
+            Real p2 = s.eke * (s.eke + 2 * rm), beta2 = p2 / (p2 + rm * rm);
+            Real ssmfp = beta2 / blccl, skindepth = T.skindepth * ssmfp;
+            tustep = dmin(tustep, dmax(tperp, skindepth));
+            bool callhowfar, dosingle = false, callmsdist;
+            Real ustep, uf, vf, wf, xf, yf, zf;
+            RT de = 0;
+            ++nstep;
+            if (tustep <= tperp && tustep > skindepth) {
+                callhowfar = false;
+                callmsdist = true;
+                de = eloss_g(T, M, qel, (RT)tustep, (RT)s.eke, (RT)s.elke, s.lelke, range, (RT)rhof);
+                msdist_pII(T, M, p, s.eke, (Real)de, tustep, rhof, uf, vf, wf, xf, yf, zf, err);
+                ustep = tustep;
+            } else {
+                callmsdist = false;
+                Real rnnoss = urand<Real>(p.rng);
+                if (rnnoss < (Real)1e-30) rnnoss = (Real)1e-30;
+                Real lambda = -dlog(1 - rnnoss);
+                Real g1 = s.eke / rm + 1;
+                Real lambda_max = (Real)0.5 * blccl * rm / dedx * g1 * g1 * g1;
+                if (lambda >= 0 && lambda_max > 0) {
+                    Real tuss = (lambda < lambda_max) ? lambda * ssmfp * (1 - (Real)0.5 * lambda / lambda_max)
+                                                       : (Real)0.5 * lambda * ssmfp;
+                    if (tuss < tustep) { tustep = tuss; dosingle = true; }
+                } else {
+                    err = 1;
+                    alive = false;
+                    continue;
+                }
+                ustep = tustep;
+                callhowfar = !(ustep < tperp);
+            }
+            int irold = p.ir, irnew = p.ir;
+            if (callhowfar) irnew = howfar(G, p.ir, p.x, p.y, p.z, p.u, p.v, p.w, ustep);
+            if (ustep <= 0) ustep = 0;
+            if (ustep == 0) {
+                if (irnew != irold) {
+                    p.ir = irnew;
+                    if (irnew < 0) {
+                        esc_tot += (double)((p.iq < 0 ? p.E - rm : p.E + rm) * p.wt);
+                        alive = false;
+                        continue;
+                    }
+                    s.medium = G.med[irnew];
+                    s.rhor = G.rhor[irnew];
+                }
+                if (p.E <= T.ecut) ecut_discard = true;
+                else { s.state = 1; continue; }
+            }
+            if (!ecut_discard) {
+                Real vstep = ustep, tvstep;
+                if (callhowfar) {
+                    tvstep = vstep;
+                    if (tvstep != tustep) dosingle = false;
+                    de = eloss_g(T, M, qel, (RT)tvstep, (RT)s.eke, (RT)s.elke, s.lelke, range, (RT)rhof);
+                } else {
+                    tvstep = tustep;
+                    if (!callmsdist) de = eloss_g(T, M, qel, (RT)tvstep, (RT)s.eke, (RT)s.elke, s.lelke, range, (RT)rhof);
+                }
+                Real edep = (Real)de, ekef = s.eke - edep;
+                if (!callmsdist) {
+                    xf = p.x + p.u * vstep; yf = p.y + p.v * vstep; zf = p.z + p.w * vstep;
+                    if (dosingle) {   // sscat (src/egsnrc.mortran:3226-3262)
+                        Real ekems = dmax(ekef, T.ecut - rm);
+                        Real pp2 = ekems * (ekems + 2 * rm);
+                        Real chia2 = M.xcc / (4 * M.blcc * pp2);
+                        Real xi = urand<Real>(p.rng);
+                        xi = 2 * chia2 * xi / (1 - xi + chia2);
+                        Real costhe = 1 - xi, sinthe = dsqrt(xi * (2 - xi));
+                        Azim<Real> az = azimuth<Real>(p.rng, err);
+                        rotate(p.u, p.v, p.w, sinthe, costhe, az, uf, vf, wf);
+                    } else { uf = p.u; vf = p.v; wf = p.w; }
+                }
+                deposit(P, acc, p.ir, p.rng.hist, (double)edep * (double)p.wt);   // AUSGAB(0)
+                edep_tot += (double)edep * (double)p.wt;
+                p.x = xf; p.y = yf; p.z = zf; p.u = uf; p.v = vf; p.w = wf;
+                p.E = p.E - edep;
+                if (irnew == p.ir && p.E <= T.ecut) ecut_discard = true;
+                else {
+                    int medold = s.medium;
+                    s.eke = p.E - rm;
+                    s.elke = dlog(s.eke);
+                    s.lelke = min(max((int)(M.eke1 * s.elke + M.eke0), 1), M.meke);
+                    if (irnew != irold) {
+                        p.ir = irnew;
+                        if (irnew < 0) {
+                            esc_tot += (double)((p.iq < 0 ? p.E - rm : p.E + rm) * p.wt);
+                            alive = false;
+                            continue;
+                        }
+                        s.medium = G.med[irnew];
+                        s.rhor = G.rhor[irnew];
+                    }
+                    if (p.E <= T.ecut) ecut_discard = true;
+                    else if (s.medium != medold) { s.state = 1; continue; }
+                    else {
+                        // $UPDATE-DEMFP (src/egsnrc.macros:3273-3281)
+                        s.demfp = s.demfp - (Real)(de * (RT)sig);
+                        s.total_de = s.total_de - de;
+                        s.total_tstep = s.total_tstep - (RT)tvstep * (RT)rhof;
+                        if (s.total_tstep < 1e-9) s.demfp = 0;
+                        if (!(s.demfp < (Real)1e-8)) continue;
+                        // fictitious-cross-section rejection
+                        const MedScalars<Real> &M2 = cmed<Real>(s.medium);
+                        ERow<Real> ef{erow(T, M2, s.lelke), qel};
+                        Real sigf = ef.sig(s.elke) / ef.dedx(s.elke);
+                        Real rfict = urand<Real>(p.rng);
+                        if (!(rfict <= sigf / s.sig0)) { s.state = 1; continue; }
+                        // discrete interaction
+                        ++ninter;
+                        const Real *rw = ef.r;
+                        bool brems = false;
+                        if (p.iq < 0) {
+                            Real ebr1 = rw[9] * s.elke + rw[8];
+                            Real r24 = urand<Real>(p.rng);
+                            brems = r24 <= ebr1;
+                            if (!brems && p.E <= M2.thmoll) {
+                                if (ebr1 <= 0) { s.state = 0; continue; }
+                                brems = true;
+                            }
+                            if (!brems) {   // MOLLER (src/egsnrc.mortran:2599-2746)
+                                Real peie = p.E, ekin = peie - rm;
+                                if (ekin <= 2 * M2.te) { s.state = 0; continue; }
+                                Real t0 = ekin / rm, e0 = t0 + 1, extrae = peie - M2.thmoll, e02 = e0 * e0;
+                                Real g2 = t0 * t0 / e02, g3 = (2 * t0 + 1) / e02, gmax = 1 + (Real)1.25 * g2, br, rejf4, r28;
+                                int it = 0;
+                                do {
+                                    Real r27 = urand<Real>(p.rng);
+                                    br = M2.te / (ekin - extrae * r27);
+                                    Real rr2 = br / (1 - br);
+                                    r28 = urand<Real>(p.rng);
+                                    rejf4 = 1 + g2 * br * br + rr2 * (rr2 - g3);
+                                    r28 = gmax * r28;
+                                    if (++it > LOOP_CAP) { err = 1; break; }
+                                } while (!(r28 <= rejf4));
+                                Real pekse2 = br * ekin, pese1 = peie - pekse2, pese2 = pekse2 + rm;
+                                Real h1 = (peie + rm) / ekin;
+                                Real dcosth = h1 * (pese1 - rm) / (pese1 + rm);
+                                Real sinthe = dsqrt(dmax((Real)0, 1 - dcosth)), costhe = dsqrt(dmin((Real)1, dcosth));
+                                Azim<Real> az = azimuth<Real>(p.rng, err);
+                                Real a = p.u, b = p.v, c = p.w;
+                                rotate(a, b, c, sinthe, costhe, az, p.u, p.v, p.w);
+                                p.E = pese1;
+                                Particle<Real> d = p;
+                                d.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
+                                dcosth = h1 * (pese2 - rm) / (pese2 + rm);
+                                sinthe = -dsqrt(dmax((Real)0, 1 - dcosth));
+                                costhe = dsqrt(dmin((Real)1, dcosth));
+                                rotate(a, b, c, sinthe, costhe, az, d.u, d.v, d.w);
+                                d.E = pese2; d.iq = -1;
+                                q_push(P, P.eout, d, npush);
+                                s.state = 0;
+                                continue;
+                            }
+                        } else {
+                            Real pbr1 = rw[11] * s.elke + rw[10];
+                            Real r25 = urand<Real>(p.rng);
+                            if (r25 < pbr1) brems = true;
+                            else {
+                                Real pbr2 = rw[13] * s.elke + rw[12];
+                                if (r25 < pbr2) {   // BHABHA (src/egsnrc.mortran:229-307)
+                                    Real peip = p.E, ekin = peip - rm, t0 = ekin / rm, e0 = t0 + 1;
+                                    Real yy = 1 / (t0 + 2), e02 = e0 * e0, beta2b = (e02 - 1) / e02;
+                                    Real ep0 = M2.te / ekin, ep0c = 1 - ep0, y2 = yy * yy, yp = 1 - 2 * yy, yp2 = yp * yp;
+                                    Real b4 = yp2 * yp, b3 = b4 + yp2, b2 = yp * (3 + y2), b1 = 2 - y2, br, rejf2, r04;
+                                    int it = 0;
+                                    do {
+                                        Real r03 = urand<Real>(p.rng);
+                                        br = ep0 / (1 - ep0c * r03);
+                                        r04 = urand<Real>(p.rng);
+                                        rejf2 = (1 - beta2b * br * (b1 - br * (b2 - br * (b3 - br * b4))));
+                                        if (++it > LOOP_CAP) { err = 1; break; }
+                                    } while (!(r04 <= rejf2));
+                                    int iq_np = 1, iq_new = -1;
+                                    if (!(br < (Real)0.5)) { iq_np = -1; iq_new = 1; br = 1 - br; }
+                                    br = dmax(br, (Real)0);
+                                    Real pekse2 = br * ekin, pese1 = peip - pekse2, pese2 = pekse2 + rm;
+                                    Real h1 = (peip + rm) / ekin;
+                                    Real dcosth = dmin((Real)1, h1 * (pese1 - rm) / (pese1 + rm));
+                                    Real sinthe = dsqrt(dmax((Real)0, 1 - dcosth)), costhe = dsqrt(dcosth);
+                                    Azim<Real> az = azimuth<Real>(p.rng, err);
+                                    Real a = p.u, b = p.v, c = p.w;
+                                    rotate(a, b, c, sinthe, costhe, az, p.u, p.v, p.w);
+                                    p.E = pese1; p.iq = iq_np;
+                                    Particle<Real> d = p;
+                                    d.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
+                                    dcosth = h1 * (pese2 - rm) / (pese2 + rm);
+                                    sinthe = -dsqrt(dmax((Real)0, 1 - dcosth));
+                                    costhe = dsqrt(dmin((Real)1, dcosth));
+                                    rotate(a, b, c, sinthe, costhe, az, d.u, d.v, d.w);
+                                    d.E = pese2; d.iq = iq_new;
+                                    q_push(P, P.eout, d, npush);
+                                    s.state = 0;
+                                    continue;
+                                }
+                                // ANNIH in flight (src/egsnrc.mortran:70-182)
+                                Real pavip = p.E + rm, avip = pavip, a = avip / rm, gg = a - 1, tt = gg - 1;
+                                Real pp = dsqrt(a * tt), pot = pp / tt, ep0 = 1 / (a + pp), wsamp = dlog((1 - ep0) / ep0);
+                                Real aa = p.u, bb = p.v, cc = p.w, ep, r02, rejf;
+                                int it = 0;
+                                do {
+                                    Real r01 = urand<Real>(p.rng);
+                                    ep = ep0 * dexp(r01 * wsamp);
+                                    r02 = urand<Real>(p.rng);
+                                    rejf = 1 - (ep * a - 1) * (ep * a - 1) / (ep * (a * a - 2));
+                                    if (++it > LOOP_CAP) { err = 1; break; }
+                                } while (!(r02 <= rejf));
+                                Real esg1 = avip * ep;
+                                Real costhe = dmax((Real)-1, dmin((Real)1, (esg1 - rm) * pot / esg1));
+                                Real sinthe = dsqrt(1 - costhe * costhe);
+                                Azim<Real> az = azimuth<Real>(p.rng, err);
+                                Particle<Real> g1 = p, g2 = p;
+                                g1.E = esg1; g1.iq = 0;
+                                rotate(aa, bb, cc, sinthe, costhe, az, g1.u, g1.v, g1.w);
+                                g2.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
+                                Real esg2 = pavip - esg1;
+                                g2.E = esg2; g2.iq = 0;
+                                costhe = dmax((Real)-1, dmin((Real)1, (esg2 - rm) * pot / esg2));
+                                sinthe = -dsqrt(1 - costhe * costhe);
+                                rotate(aa, bb, cc, sinthe, costhe, az, g2.u, g2.v, g2.w);
+                                q_push(P, P.pout, g1, npush);
+                                q_push(P, P.pout, g2, npush);
+                                alive = false;
+                                continue;
+                            }
+                        }
+                        // BREMS, BH cross section with KM angles (src/egsnrc.mortran:312-524)
+                        {
+                            Real peie = p.E, ekin = peie - rm, brmin = M2.ap / ekin, waux = s.elke - M2.log_ap;
+                            int l = (peie < 50) ? 0 : 2, l1 = l + 1;
+                            Real a = p.u, b = p.v, c = p.w, sinpsi = a * a + b * b, sindel = 0, cosdel = 0;
+                            if (sinpsi > (Real)1e-20) { sinpsi = dsqrt(sinpsi); sindel = b / sinpsi; cosdel = a / sinpsi; }
+                            Real tteie = peie / rm;
+                            Real beta = dsqrt((tteie - 1) * (tteie + 1)) / tteie;
+                            Real y2max = 2 * beta * (1 + beta) * tteie * tteie, y2maxi = 1 / y2max;
+                            Real z2maxi = dsqrt(y2max + 1);
+                            Real esg, ese, r07, rejf;
+                            int it = 0;
+                            do {
+                                Real r06 = urand<Real>(p.rng);
+                                r07 = urand<Real>(p.rng);
+                                Real br = brmin * dexp(r06 * waux);
+                                esg = ekin * br;
+                                ese = peie - esg;
+                                Real delta = esg / peie / ese * M2.delcm, aux = ese / peie, phi1, phi2;
+                                if (delta < 1) {
+                                    phi1 = M2.dl[0][l] + delta * (M2.dl[1][l] + delta * M2.dl[2][l]);
+                                    phi2 = M2.dl[0][l1] + delta * (M2.dl[1][l1] + delta * M2.dl[2][l1]);
+                                } else {
+                                    phi1 = M2.dl[3][l] + M2.dl[4][l] * dlog(delta + M2.dl[5][l]);
+                                    phi2 = phi1;
+                                }
+                                rejf = (1 + aux * aux) * phi1 - 2 * aux * phi2 / 3;
+                                if (++it > LOOP_CAP) { err = 1; break; }
+                            } while (!(r07 < rejf));
+                            Real ttese = ese / rm, esedei = ttese / tteie, rjarg1 = 1 + esedei * esedei;
+                            Real rjarg2 = rjarg1 + 2 * esedei;
+                            Real aux = 2 * ese * tteie / esg;
+                            aux = aux * aux;
+                            Real aux1 = aux * M2.zbrang, rjarg3;
+                            if (aux1 > 10) rjarg3 = M2.lzbrang + (1 - aux1) / (aux1 * aux1);
+                            else rjarg3 = dlog(aux / (1 + aux1));
+                            Real rejmax = rjarg1 * rjarg3 - rjarg2, y2tst, rtest;
+                            it = 0;
+                            while (true) {
+                                y2tst = urand<Real>(p.rng);
+                                rtest = urand<Real>(p.rng);
+                                Real aux3 = z2maxi / (y2tst + (1 - y2tst) * z2maxi);
+                                rtest = rtest * aux3 * rejmax;
+                                y2tst = aux3 * aux3 - 1;
+                                Real a34 = aux3 * aux3 * aux3 * aux3;
+                                Real y2tst1 = esedei * y2tst / a34;
+                                Real aux4 = 16 * y2tst1 - rjarg2, aux5 = rjarg1 - 4 * y2tst1;
+                                if (rtest < aux4 + aux5 * rjarg3) break;
+                                Real aux2 = dlog(aux / (1 + aux1 / a34));
+                                Real rejtst = aux4 + aux5 * aux2;
+                                if (rtest < rejtst) break;
+                                if (++it > LOOP_CAP) { err = 1; break; }
+                            }
+                            Real costhe = 1 - 2 * y2tst * y2maxi;
+                            Real sinthe = dsqrt(dmax((1 - costhe) * (1 + costhe), (Real)0));
+                            Azim<Real> az = azimuth<Real>(p.rng, err);
+                            Particle<Real> gph = p;
+                            gph.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
+                            gph.E = esg; gph.iq = 0;
+                            if (sinpsi >= (Real)1e-10) {
+                                Real us = sinthe * az.c, vs = sinthe * az.s;
+                                gph.u = c * cosdel * us - sindel * vs + a * costhe;
+                                gph.v = c * sindel * us + cosdel * vs + b * costhe;
+                                gph.w = c * costhe - sinpsi * us;
+                            } else { gph.u = sinthe * az.c; gph.v = sinthe * az.s; gph.w = c * costhe; }
+                            q_push(P, P.pout, gph, npush);
+                            p.E = ese;
+                            s.state = 0;
+                            continue;
+                        }
+                    }
+                }
+            }
+        }
+        // :ECUT-DISCARD: (src/egsnrc.mortran:1768-1802)
+        {
+            Real edep = p.E - rm;
+            deposit(P, acc, p.ir, p.rng.hist, (double)(edep * p.wt));
+            edep_tot += (double)(edep * p.wt);
+            if (p.iq > 0) {   // ANNIH_AT_REST (src/egsnrc.mortran:186-223)
+                Real costhe = urand<Real>(p.rng);
+                costhe = 2 * costhe - 1;
+                Real sinthe = dsqrt(dmax((Real)0, (1 - costhe) * (1 + costhe)));
+                Azim<Real> az = azimuth<Real>(p.rng, err);
+                Particle<Real> g1 = p, g2 = p;
+                g1.E = rm; g1.iq = 0; g1.u = sinthe * az.c; g1.v = sinthe * az.s; g1.w = costhe;
+                g2.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
+                g2.E = rm; g2.iq = 0; g2.u = -g1.u; g2.v = -g1.v; g2.w = -g1.w;
+                q_push(P, P.pout, g1, npush);
+                q_push(P, P.pout, g2, npush);
+            }
+            alive = false;
+        }
+    }
+    acc_flush(P, acc);
+    for (int o = 16; o > 0; o >>= 1) {
+        nstep += __shfl_down_sync(0xffffffffu, nstep, o);
+        npush += __shfl_down_sync(0xffffffffu, npush, o);
+        ninter += __shfl_down_sync(0xffffffffu, ninter, o);
+        edep_tot += __shfl_down_sync(0xffffffffu, edep_tot, o);
+        esc_tot += __shfl_down_sync(0xffffffffu, esc_tot, o);
+    }
+    if (lane == 0) {
+        atomicAdd(P.counters + CNT_ESTEP, nstep);
+        atomicAdd(P.counters + CNT_PUSH, npush);
+        atomicAdd(P.counters + CNT_INTER, ninter);
+        atomicAdd(P.energy + 0, edep_tot);
+        atomicAdd(P.energy + 1, esc_tot);
+    }
+    if (err) atomicExch(P.error + 1, 1);
+}
+
+// Batch fold: sum += d, sum2 += d*d, d = 0 (DOSXYZnrc batch statistics).
+__global__ void k_batch(double *d, double *sum, double *sum2, long long n) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += stride) {
+        double x = d[i];
+        sum[i] += x;
+        sum2[i] += x * x;
+        d[i] = 0;
+    }
+}
+
+}  // namespace egsgpu
+
+// ===================================================================
+//                         host-side engine
+// ===================================================================
+using namespace egsgpu;
+
+namespace {
+
+#define CK(x)                                                                                 \
+    do {                                                                                      \
+        cudaError_t e_ = (x);                                                                 \
+        if (e_ != cudaSuccess) {                                                              \
+            err = std::string(#x) + ": " + cudaGetErrorString(e_);                            \
+            return EGSGPU_ERR_CUDA;                                                           \
+        }                                                                                     \
+    } while (0)
+
+struct DevMem {
+    void *p = nullptr;
+    size_t n = 0;
+    ~DevMem() { if (p) cudaFree(p); }
+    cudaError_t alloc(size_t bytes) {
+        if (p) { cudaFree(p); p = nullptr; }
+        n = bytes;
+        return cudaMalloc(&p, bytes ? bytes : 16);
+    }
+};
+
+struct EngineBase {
+    virtual ~EngineBase() {}
+    virtual int load(const egs::Hatch &H, double ecut, double pcut, double skindepth, std::string &err) = 0;
+    virtual int geometry(int nx, int ny, int nz, const double *xb, const double *yb, const double *zb,
+                         const int32_t *med, const double *rhor, std::string &err) = 0;
+    virtual int run(const Source &S, long long first, long long n, int nbatch, uint32_t seed, cudaStream_t st,
+                    std::string &err) = 0;
+};
+
+template <class Real>
+struct Engine : EngineBase {
+    egsgpu_config cfg;
+    int nmed = 0;
+    std::vector<MedScalars<Real>> meds;
+    DevMem d_etab, d_erange, d_gtab, d_pmax, d_ray, d_rayi, d_shell, d_shellat, d_elem, d_ms, d_msi;
+    Tables<Real> T{};
+    // geometry
+    Geom<Real> G{};
+    DevMem d_xb, d_yb, d_zb, d_med, d_rhor;
+    long long nvox = 0;
+    // queues: P[2], E[2]
+    DevMem qmem[4];
+    Queue<Real> q[4];
+    DevMem d_counts;   // 4 queues x (count, head)
+    unsigned capacity = 0;
+    // tallies
+    DevMem d_dose, d_sum, d_sum2, d_energy, d_counters, d_error, d_hist;
+    long long hist_first = 0, hist_n = 0;
+    int sm_count = 0;
+
+    explicit Engine(const egsgpu_config &c) : cfg(c) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev);
+    }
+
+    int load(const egs::Hatch &H, double ecut, double pcut, double skindepth, std::string &err) override {
+        nmed = (int)H.media.size();
+        if (nmed > MAXMED) { err = "too many media"; return EGSGPU_ERR_ARG; }
+        std::vector<Real> etab, gtab, pmax, ray, shell, elem, ms;
+        std::vector<RT> erange;
+        std::vector<int> rayi, shellat, msi;
+        meds.assign(nmed, MedScalars<Real>());
+        int eoff = 0, goff = 0, soff = 0, loff = 0;
+        for (int im = 0; im < nmed; ++im) {
+            const egs::Medium &m = H.media[im];
+            MedScalars<Real> &M = meds[im];
+            std::memset(&M, 0, sizeof(M));
+            M.rho = (Real)m.rho; M.ae = (Real)m.ae; M.ap = (Real)m.ap; M.te = (Real)m.te;
+            M.thmoll = (Real)m.thmoll; M.blcc = (Real)m.blcc; M.xcc = (Real)m.xcc;
+            M.eke0 = (Real)m.eke0; M.eke1 = (Real)m.eke1; M.ge0 = (Real)m.ge0; M.ge1 = (Real)m.ge1;
+            M.esig_e = (Real)m.esig_e; M.psig_e = (Real)m.psig_e; M.log_ap = (Real)m.log_ap;
+            M.delcm = (Real)m.delcm; M.zbrang = (Real)m.zbrang; M.lzbrang = (Real)m.lzbrang;
+            for (int k = 0; k < 6; ++k)
+                for (int l = 0; l < 8; ++l) M.dl[k][l] = (Real)m.dl[k][l];
+            M.bpar[0] = (Real)m.bpar[0]; M.bpar[1] = (Real)m.bpar[1];
+            M.E_array0 = m.E_array[0];
+            M.meke = m.meke; M.n_shell = m.n_shell; M.nne = m.nne;
+            M.sig_mono_e = m.sig_ismonotone[0]; M.sig_mono_p = m.sig_ismonotone[1];
+            M.etab_off = eoff; M.gtab_off = goff; M.shell_off = soff; M.elem_off = loff;
+            if (m.nne > MAXNE) { err = "too many elements in medium " + m.name; return EGSGPU_ERR_ARG; }
+            for (int k = 0; k < m.nne; ++k) M.pz[k] = (float)m.pz[k];
+            for (int i = 0; i < m.meke; ++i) {
+                const double v[16] = {m.esig0[i], m.esig1[i], m.psig0[i], m.psig1[i], m.ededx0[i], m.ededx1[i],
+                                      m.pdedx0[i], m.pdedx1[i], m.ebr10[i], m.ebr11[i], m.pbr10[i], m.pbr11[i],
+                                      m.pbr20[i], m.pbr21[i], m.tmxs0[i], m.tmxs1[i]};
+                for (double x : v) etab.push_back((Real)x);
+                erange.push_back(m.E_array[i]); erange.push_back(m.range_ep0[i]);
+                erange.push_back(m.range_ep1[i]); erange.push_back(0);
+            }
+            eoff += m.meke;
+            for (int i = 0; i < m.mge; ++i) {
+                const double v[8] = {m.gmfp0[i], m.gmfp1[i], m.gbr10[i], m.gbr11[i],
+                                     m.gbr20[i], m.gbr21[i], m.cohe0[i], m.cohe1[i]};
+                for (double x : v) gtab.push_back((Real)x);
+                pmax.push_back((Real)m.pmax0[i]); pmax.push_back((Real)m.pmax1[i]);
+            }
+            if (m.mge != MXGE) { err = "unexpected photon grid size"; return EGSGPU_ERR_DATA; }
+            goff += m.mge;
+            for (int i = 0; i < NRAY; ++i) ray.push_back((Real)m.xgrid[i]);
+            for (int i = 0; i < NRAY; ++i) ray.push_back((Real)m.fcum[i]);
+            for (int i = 0; i < NRAY; ++i) ray.push_back((Real)m.b_array[i]);
+            for (int i = 0; i < NRAY; ++i) ray.push_back((Real)m.c_array[i]);
+            for (int i = 0; i < NRAY; ++i) rayi.push_back(m.i_array[i]);
+            for (int i = 0; i < m.n_shell; ++i) {
+                int j = m.shell_array[i];
+                shell.push_back((Real)m.eno_array[i]); shell.push_back((Real)H.shells.be[j]);
+                shell.push_back((Real)H.shells.Jo[j]); shell.push_back((Real)H.shells.erfJo[j]);
+                shellat.push_back(m.eno_atbin_array[i]);
+            }
+            soff += m.n_shell;
+            for (int k = 0; k < m.nne; ++k) {
+                const egs::ElementPhoto &e = H.elements[m.elem_index[k]];
+                Real row[96] = {};
+                for (int j = 0; j < 16; ++j) {
+                    row[j] = (Real)e.edge_a[j]; row[16 + j] = (Real)e.edge_b[j]; row[32 + j] = (Real)e.edge_c[j];
+                    row[48 + j] = (Real)e.edge_d[j]; row[64 + j] = (Real)e.edge_energies[j];
+                }
+                for (int j = 0; j < 6; ++j) { row[80 + j] = (Real)e.binding[j]; row[86 + j] = (Real)e.interaction_prob[j]; }
+                row[95] = (Real)e.edge_number;
+                elem.insert(elem.end(), row, row + 96);
+            }
+            loff += m.nne;
+        }
+        for (size_t i = 0; i < H.ums.size(); ++i) {
+            ms.push_back((Real)H.ums[i]); ms.push_back((Real)H.fms[i]); ms.push_back((Real)H.wms[i]);
+            msi.push_back(H.ims[i]);
+        }
+        auto up = [&](DevMem &d, const void *src, size_t bytes) -> cudaError_t {
+            cudaError_t e = d.alloc(bytes);
+            if (e != cudaSuccess) return e;
+            return cudaMemcpy(d.p, src, bytes, cudaMemcpyHostToDevice);
+        };
+        CK(up(d_etab, etab.data(), etab.size() * sizeof(Real)));
+        CK(up(d_erange, erange.data(), erange.size() * sizeof(RT)));
+        CK(up(d_gtab, gtab.data(), gtab.size() * sizeof(Real)));
+        CK(up(d_pmax, pmax.data(), pmax.size() * sizeof(Real)));
+        CK(up(d_ray, ray.data(), ray.size() * sizeof(Real)));
+        CK(up(d_rayi, rayi.data(), rayi.size() * sizeof(int)));
+        CK(up(d_shell, shell.data(), shell.size() * sizeof(Real)));
+        CK(up(d_shellat, shellat.data(), shellat.size() * sizeof(int)));
+        CK(up(d_elem, elem.data(), elem.size() * sizeof(Real)));
+        CK(up(d_ms, ms.data(), ms.size() * sizeof(Real)));
+        CK(up(d_msi, msi.data(), msi.size() * sizeof(int)));
+        if (sizeof(Real) == 4) CK(cudaMemcpyToSymbol(c_med_f, meds.data(), nmed * sizeof(MedScalars<Real>)));
+        else CK(cudaMemcpyToSymbol(c_med_d, meds.data(), nmed * sizeof(MedScalars<Real>)));
+        T.etab = (const Real *)d_etab.p; T.erange = (const RT *)d_erange.p; T.gtab = (const Real *)d_gtab.p;
+        T.pmax = (const Real *)d_pmax.p; T.ray = (const Real *)d_ray.p; T.ray_i = (const int *)d_rayi.p;
+        T.shell = (const Real *)d_shell.p; T.shell_at = (const int *)d_shellat.p; T.elem = (const Real *)d_elem.p;
+        T.ms = (const Real *)d_ms.p; T.ms_i = (const int *)d_msi.p;
+        T.dllambi = (Real)H.dllambi; T.dqmsi = (Real)H.dqmsi;
+        T.nmed = nmed;
+        T.ecut = (Real)ecut; T.pcut = (Real)pcut; T.skindepth = (Real)skindepth; T.smaxir = (Real)1e10;
+        // tallies that do not depend on the geometry
+        CK(d_energy.alloc(2 * sizeof(double)));
+        CK(d_counters.alloc(CNT_N * sizeof(unsigned long long)));
+        CK(d_error.alloc(2 * sizeof(int)));
+        CK(cudaMemset(d_energy.p, 0, 2 * sizeof(double)));
+        CK(cudaMemset(d_counters.p, 0, CNT_N * sizeof(unsigned long long)));
+        CK(cudaMemset(d_error.p, 0, 2 * sizeof(int)));
+        return 0;
+    }
+
+    int geometry(int nx, int ny, int nz, const double *xb, const double *yb, const double *zb, const int32_t *med,
+                 const double *rhor, std::string &err) override {
+        nvox = (long long)nx * ny * nz;
+        std::vector<Real> x(xb, xb + nx + 1), y(yb, yb + ny + 1), z(zb, zb + nz + 1), r(nvox);
+        std::vector<uint8_t> m(nvox);
+        for (long long i = 0; i < nvox; ++i) { m[i] = (uint8_t)med[i]; r[i] = (Real)rhor[i]; }
+        auto up = [&](DevMem &d, const void *src, size_t bytes) -> cudaError_t {
+            cudaError_t e = d.alloc(bytes);
+            if (e != cudaSuccess) return e;
+            return cudaMemcpy(d.p, src, bytes, cudaMemcpyHostToDevice);
+        };
+        CK(up(d_xb, x.data(), x.size() * sizeof(Real)));
+        CK(up(d_yb, y.data(), y.size() * sizeof(Real)));
+        CK(up(d_zb, z.data(), z.size() * sizeof(Real)));
+        CK(up(d_med, m.data(), m.size()));
+        CK(up(d_rhor, r.data(), r.size() * sizeof(Real)));
+        G.nx = nx; G.ny = ny; G.nz = nz; G.nxy = nx * ny;
+        G.xb = (const Real *)d_xb.p; G.yb = (const Real *)d_yb.p; G.zb = (const Real *)d_zb.p;
+        G.med = (const uint8_t *)d_med.p; G.rhor = (const Real *)d_rhor.p;
+        // egs++ distanceEpsilon: 2^-32 cm in FP64, 2^-21 cm in FP32 (egs++/egs_functions.h:80-88)
+        G.bt = sizeof(Real) == 8 ? (Real)(1.0 / 4294967296.0) : (Real)(1.0 / 2097152.0);
+        G.hbt = G.bt / 2;
+        CK(d_dose.alloc(nvox * sizeof(double)));
+        CK(d_sum.alloc(nvox * sizeof(double)));
+        CK(d_sum2.alloc(nvox * sizeof(double)));
+        CK(cudaMemset(d_dose.p, 0, nvox * sizeof(double)));
+        CK(cudaMemset(d_sum.p, 0, nvox * sizeof(double)));
+        CK(cudaMemset(d_sum2.p, 0, nvox * sizeof(double)));
+        return 0;
+    }
+
+    int ensure_queues(unsigned cap, std::string &err) {
+        if (cap <= capacity) return 0;
+        size_t per = 8 * sizeof(Real) + sizeof(int) + sizeof(int8_t) + 2 * sizeof(uint32_t) + sizeof(unsigned long long);
+        CK(d_counts.alloc(8 * sizeof(unsigned)));
+        for (int k = 0; k < 4; ++k) {
+            CK(qmem[k].alloc((size_t)cap * per + 1024));
+            char *b = (char *)qmem[k].p;
+            auto take = [&](size_t bytes) { char *r = b; b += (bytes + 255) & ~(size_t)255; return r; };
+            Queue<Real> &Q = q[k];
+            Q.x = (Real *)take(cap * sizeof(Real)); Q.y = (Real *)take(cap * sizeof(Real));
+            Q.z = (Real *)take(cap * sizeof(Real)); Q.u = (Real *)take(cap * sizeof(Real));
+            Q.v = (Real *)take(cap * sizeof(Real)); Q.w = (Real *)take(cap * sizeof(Real));
+            Q.E = (Real *)take(cap * sizeof(Real)); Q.wt = (Real *)take(cap * sizeof(Real));
+            Q.ir = (int *)take(cap * sizeof(int));
+            Q.iq = (k >= 2) ? (int8_t *)take(cap) : nullptr;
+            Q.hist = (uint32_t *)take(cap * sizeof(uint32_t)); Q.n = (uint32_t *)take(cap * sizeof(uint32_t));
+            Q.sid = (unsigned long long *)take(cap * sizeof(unsigned long long));
+            Q.count = (unsigned *)d_counts.p + 2 * k;
+            Q.capacity = cap;
+        }
+        capacity = cap;
+        return 0;
+    }
+
+    int run(const Source &S, long long first, long long n, int nbatch, uint32_t seed, cudaStream_t st,
+            std::string &err) override {
+        if (!G.xb) { err = "geometry not set"; return EGSGPU_ERR_STATE; }
+        unsigned cap = cfg.capacity > 0 ? (unsigned)std::min<long long>(cfg.capacity, 0x7fffffffLL) : (1u << 24);
+        if (int rc = ensure_queues(cap, err)) return rc;
+        long long chunk = cfg.chunk;
+        if (chunk <= 0) {
+            double emax = S.spectrum == 0 ? S.energy : 20.0;
+            double per = (S.charge == 0 ? 12.0 : 16.0) + 8.0 * emax;
+            chunk = std::max<long long>(1024, (long long)(capacity / per));
+        }
+        const int bs = cfg.block_size > 0 ? cfg.block_size : 128;
+        const int cps = cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm : 8;
+        const int grid = sm_count * cps;
+        Params<Real> P;
+        P.T = T; P.G = G;
+        P.dose = (double *)d_dose.p;
+        P.hist_tally = hist_n > 0 ? (double *)d_hist.p : nullptr;
+        P.hist_first = hist_first; P.hist_n = hist_n;
+        P.energy = (double *)d_energy.p;
+        P.counters = (unsigned long long *)d_counters.p;
+        P.error = (int *)d_error.p;
+        P.seed = seed;
+        unsigned *counts = (unsigned *)d_counts.p;
+        long long per_batch = n / nbatch;
+        for (int b = 0; b < nbatch; ++b) {
+            long long b0 = first + b * per_batch, bn = (b == nbatch - 1) ? n - b * per_batch : per_batch;
+            for (long long c0 = b0; c0 < b0 + bn; c0 += chunk) {
+                long long cn = std::min(chunk, b0 + bn - c0);
+                int cur = 0;
+                CK(cudaMemsetAsync(counts, 0, 8 * sizeof(unsigned), st));
+                P.pout = q[0]; P.eout = q[2];
+                k_source<Real><<<(unsigned)((cn + 255) / 256), 256, 0, st>>>(P, S, c0, cn);
+                CK(cudaGetLastError());
+                for (int round = 0; round < 100000; ++round) {
+                    unsigned h[8];
+                    CK(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, st));
+                    CK(cudaStreamSynchronize(st));
+                    unsigned np = h[2 * cur], ne = h[4 + 2 * cur];
+                    if (np > capacity || ne > capacity) {
+                        err = "particle queue capacity exceeded; lower egsgpu_config.chunk or raise capacity";
+                        return EGSGPU_ERR_CAPACITY;
+                    }
+                    if (np == 0 && ne == 0) break;
+                    int nxt = 1 - cur;
+                    // next queues start empty
+                    CK(cudaMemsetAsync(counts + 2 * nxt, 0, 2 * sizeof(unsigned), st));
+                    CK(cudaMemsetAsync(counts + 4 + 2 * nxt, 0, 2 * sizeof(unsigned), st));
+                    if (np) {
+                        P.pin = q[cur]; P.ein = q[2 + cur];
+                        int g = (int)std::min<long long>(grid, (np + bs - 1) / bs);
+                        k_photon<Real><<<g, bs, 0, st>>>(P);
+                        CK(cudaGetLastError());
+                    }
+                    CK(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, st));
+                    CK(cudaStreamSynchronize(st));
+                    ne = h[4 + 2 * cur];
+                    if (ne > capacity) {
+                        err = "particle queue capacity exceeded; lower egsgpu_config.chunk or raise capacity";
+                        return EGSGPU_ERR_CAPACITY;
+                    }
+                    if (ne) {
+                        P.ein = q[2 + cur]; P.pout = q[nxt]; P.eout = q[2 + nxt];
+                        int g = (int)std::min<long long>(grid, (ne + bs - 1) / bs);
+                        k_electron<Real><<<g, bs, 0, st>>>(P);
+                        CK(cudaGetLastError());
+                    }
+                    cur = nxt;
+                }
+            }
+            k_batch<<<std::max(1, std::min(4 * sm_count, (int)((nvox + 255) / 256))), 256, 0, st>>>(
+                (double *)d_dose.p, (double *)d_sum.p, (double *)d_sum2.p, nvox);
+            CK(cudaGetLastError());
+        }
+        CK(cudaStreamSynchronize(st));
+        int e[2];
+        CK(cudaMemcpy(e, d_error.p, sizeof(e), cudaMemcpyDeviceToHost));
+        if (e[0]) { err = "particle queue capacity exceeded"; return EGSGPU_ERR_CAPACITY; }
+        if (e[1]) { err = "a device sampling loop hit its iteration cap"; return EGSGPU_ERR_LOOP; }
+        return 0;
+    }
+};
+
+}  // namespace
+
+struct egsgpu_handle {
+    egsgpu_config cfg;
+    std::string err;
+    egs::Hatch H;
+    bool have_media = false, have_geom = false, have_source = false;
+    std::unique_ptr<EngineBase> eng;
+    // geometry copies for dose normalisation
+    int nx = 0, ny = 0, nz = 0;
+    std::vector<double> xb, yb, zb, rhor;
+    std::vector<int32_t> med;
+    // source
+    Source S{};
+    DevMem d_edges, d_wi, d_bin;
+    long long nhist = 0;
+    int nbatch = 0;
+    double ecut = 0, pcut = 0;
+};
+
+template <class E>
+static int get_tallies_impl(egsgpu_handle *h, E *eng, double *sum, double *sum2, double *totals) {
+    std::string &err = h->err;
+    long long nv = (long long)h->nx * h->ny * h->nz;
+    if (sum) CK(cudaMemcpy(sum, eng->d_sum.p, nv * sizeof(double), cudaMemcpyDeviceToHost));
+    if (sum2) CK(cudaMemcpy(sum2, eng->d_sum2.p, nv * sizeof(double), cudaMemcpyDeviceToHost));
+    if (totals) {
+        double en[2];
+        unsigned long long c[CNT_N];
+        CK(cudaMemcpy(en, eng->d_energy.p, sizeof(en), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(c, eng->d_counters.p, sizeof(c), cudaMemcpyDeviceToHost));
+        totals[0] = (double)h->nhist; totals[1] = h->nbatch; totals[2] = en[0]; totals[3] = en[1];
+        totals[4] = (double)(c[CNT_PSTEP] + c[CNT_ESTEP]); totals[5] = (double)c[CNT_PSTEP];
+        totals[6] = (double)c[CNT_ESTEP]; totals[7] = (double)c[CNT_PUSH];
+    }
+    return 0;
+}
+
+extern "C" {
+
+void egsgpu_default_config(egsgpu_config *c) {
+    std::memset(c, 0, sizeof(*c));
+    c->ecut = 0.521; c->pcut = 0.010;
+    c->estepe = 0.25; c->ximax = 0.5; c->skindepth = 3.0;
+    c->precision = 32;
+}
+
+int egsgpu_create(const egsgpu_config *cfg, egsgpu_handle **out) {
+    if (!cfg || !out) return EGSGPU_ERR_ARG;
+    *out = nullptr;
+    if (cfg->precision != 32 && cfg->precision != 64) return EGSGPU_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return EGSGPU_ERR_CUDA;
+    auto *h = new egsgpu_handle();
+    h->cfg = *cfg;
+    if (cfg->precision == 32) h->eng.reset(new Engine<float>(*cfg));
+    else h->eng.reset(new Engine<double>(*cfg));
+    *out = h;
+    return 0;
+}
+
+int egsgpu_load_media(egsgpu_handle *h, const char *data_dir, const char *pegs_file, const char *const *names,
+                      int n) {
+    if (!h || !data_dir || !pegs_file || !names || n < 1) return EGSGPU_ERR_ARG;
+    egs::TransportParams tp;
+    tp.ecut = h->cfg.ecut; tp.pcut = h->cfg.pcut;
+    tp.estepe = h->cfg.estepe; tp.ximax = h->cfg.ximax; tp.skindepth_for_bca = h->cfg.skindepth;
+    std::vector<std::string> nm;
+    for (int i = 0; i < n; ++i) nm.push_back(names[i]);
+    int rc = egs::hatch(data_dir, pegs_file, nm, tp, h->H, h->err);
+    if (rc) return rc;
+    // $adjust_rhor_ecut_pcut: cut-offs not below any AE / AP
+    double ecut = h->cfg.ecut, pcut = h->cfg.pcut;
+    for (auto &m : h->H.media) { ecut = std::max(ecut, m.ae); pcut = std::max(pcut, m.ap); }
+    // Relaxation products are deposited locally: exact only while every shell
+    // binding energy is below both transport cut-offs.
+    if (h->H.max_binding_energy > std::min(pcut, ecut - egs::RM)) {
+        h->err = "a shell binding energy exceeds the cut-offs: relaxation cascades above cut-off are not supported";
+        return EGSGPU_ERR_ARG;
+    }
+    h->ecut = ecut; h->pcut = pcut;
+    rc = h->eng->load(h->H, ecut, pcut, h->cfg.skindepth, h->err);
+    if (rc) return rc;
+    h->have_media = true;
+    return 0;
+}
+
+int egsgpu_set_xyz_geometry(egsgpu_handle *h, int nx, int ny, int nz, const double *xb, const double *yb,
+                            const double *zb, const int32_t *med, const double *rhor) {
+    if (!h || nx < 1 || ny < 1 || nz < 1 || !xb || !yb || !zb || !med || !rhor) return EGSGPU_ERR_ARG;
+    if (!h->have_media) { h->err = "load media before the geometry"; return EGSGPU_ERR_STATE; }
+    long long nv = (long long)nx * ny * nz;
+    if (nv > (1LL << 31) - 1) { h->err = "too many voxels"; return EGSGPU_ERR_ARG; }
+    for (int i = 0; i < nx; ++i) if (!(xb[i + 1] > xb[i])) { h->err = "x-planes not increasing"; return EGSGPU_ERR_ARG; }
+    for (int i = 0; i < ny; ++i) if (!(yb[i + 1] > yb[i])) { h->err = "y-planes not increasing"; return EGSGPU_ERR_ARG; }
+    for (int i = 0; i < nz; ++i) if (!(zb[i + 1] > zb[i])) { h->err = "z-planes not increasing"; return EGSGPU_ERR_ARG; }
+    int nmed = (int)h->H.media.size();
+    for (long long i = 0; i < nv; ++i) {
+        if (med[i] < 0 || med[i] >= nmed) { h->err = "voxel medium index out of range"; return EGSGPU_ERR_ARG; }
+        if (!(rhor[i] > 0) || !std::isfinite(rhor[i])) { h->err = "voxel relative density must be positive and finite"; return EGSGPU_ERR_ARG; }
+    }
+    int rc = h->eng->geometry(nx, ny, nz, xb, yb, zb, med, rhor, h->err);
+    if (rc) return rc;
+    h->nx = nx; h->ny = ny; h->nz = nz;
+    h->xb.assign(xb, xb + nx + 1); h->yb.assign(yb, yb + ny + 1); h->zb.assign(zb, zb + nz + 1);
+    h->med.assign(med, med + nv); h->rhor.assign(rhor, rhor + nv);
+    h->have_geom = true;
+    h->nhist = 0; h->nbatch = 0;
+    return 0;
+}
+
+int egsgpu_set_source(egsgpu_handle *h, const egsgpu_source *s) {
+    if (!h || !s) return EGSGPU_ERR_ARG;
+    if (s->charge < -1 || s->charge > 1 || (s->shape != 0 && s->shape != 1) || (s->spectrum != 0 && s->spectrum != 1)) {
+        h->err = "unsupported source";
+        return EGSGPU_ERR_ARG;
+    }
+    double nrm = std::sqrt(s->dir[0] * s->dir[0] + s->dir[1] * s->dir[1] + s->dir[2] * s->dir[2]);
+    if (!(nrm > 0)) { h->err = "zero source direction"; return EGSGPU_ERR_ARG; }
+    Source S{};
+    S.charge = s->charge; S.shape = s->shape; S.spectrum = s->spectrum;
+    for (int k = 0; k < 3; ++k) { S.pos[k] = s->pos[k]; S.dir[k] = s->dir[k] / nrm; }
+    S.xmin = s->xmin; S.xmax = s->xmax; S.ymin = s->ymin; S.ymax = s->ymax;
+    S.energy = s->energy;
+    if (s->spectrum == 0) {
+        if (!(s->energy > 0)) { h->err = "source energy must be positive"; return EGSGPU_ERR_ARG; }
+    } else {
+        int nb = s->nbins;
+        if (nb < 1 || !s->edges || !s->weights) { h->err = "bad spectrum"; return EGSGPU_ERR_ARG; }
+        // Walker alias table over histogram bins (egs++/egs_alias_table.cpp:117-263)
+        std::vector<double> w(nb), wi(nb, 1.0);
+        std::vector<int> bin(nb, 0);
+        double sum = 0;
+        for (int i = 0; i < nb; ++i) {
+            if (!(s->edges[i + 1] > s->edges[i]) || s->weights[i] < 0) { h->err = "bad spectrum bins"; return EGSGPU_ERR_ARG; }
+            w[i] = s->weights[i] * (s->edges[i + 1] - s->edges[i]);
+            sum += w[i];
+        }
+        if (!(sum > 0)) { h->err = "empty spectrum"; return EGSGPU_ERR_ARG; }
+        for (int i = 0; i < nb; ++i) w[i] = w[i] / sum * nb;
+        std::vector<int> small, large;
+        for (int i = 0; i < nb; ++i) (w[i] < 1 ? small : large).push_back(i);
+        while (!small.empty() && !large.empty()) {
+            int sm = small.back(); small.pop_back();
+            int lg = large.back();
+            wi[sm] = w[sm]; bin[sm] = lg;
+            w[lg] -= 1 - w[sm];
+            if (w[lg] < 1) { large.pop_back(); small.push_back(lg); }
+        }
+        for (int i : small) { wi[i] = 1; bin[i] = i; }
+        for (int i : large) { wi[i] = 1; bin[i] = i; }
+        std::string &err = h->err;
+        CK(h->d_edges.alloc((nb + 1) * sizeof(double)));
+        CK(h->d_wi.alloc(nb * sizeof(double)));
+        CK(h->d_bin.alloc(nb * sizeof(int)));
+        CK(cudaMemcpy(h->d_edges.p, s->edges, (nb + 1) * sizeof(double), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(h->d_wi.p, wi.data(), nb * sizeof(double), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(h->d_bin.p, bin.data(), nb * sizeof(int), cudaMemcpyHostToDevice));
+        S.nbins = nb;
+        S.edges = (const double *)h->d_edges.p; S.wi = (const double *)h->d_wi.p; S.bin = (const int *)h->d_bin.p;
+    }
+    h->S = S;
+    h->have_source = true;
+    return 0;
+}
+
+int egsgpu_run(egsgpu_handle *h, long long first, long long n, int n_batch, uint32_t seed, void *stream) {
+    if (!h || n < 0 || n_batch < 1 || first < 0 || first + n > 0xffffffffLL) return EGSGPU_ERR_ARG;
+    if (!h->have_media || !h->have_geom || !h->have_source) { h->err = "media, geometry and source must be set"; return EGSGPU_ERR_STATE; }
+    if (n == 0) return 0;
+    if (n_batch > n) n_batch = (int)n;
+    int rc = h->eng->run(h->S, first, n, n_batch, seed, (cudaStream_t)stream, h->err);
+    if (rc) return rc;
+    h->nhist += n;
+    h->nbatch += n_batch;
+    return 0;
+}
+
+int egsgpu_reset(egsgpu_handle *h) {
+    if (!h || !h->have_geom) return EGSGPU_ERR_STATE;
+    std::string &err = h->err;
+    EngineBase *e = h->eng.get();
+    (void)e;
+    long long nv = (long long)h->nx * h->ny * h->nz;
+    auto reset = [&](auto *eng) -> int {
+        CK(cudaMemset(eng->d_dose.p, 0, nv * sizeof(double)));
+        CK(cudaMemset(eng->d_sum.p, 0, nv * sizeof(double)));
+        CK(cudaMemset(eng->d_sum2.p, 0, nv * sizeof(double)));
+        CK(cudaMemset(eng->d_energy.p, 0, 2 * sizeof(double)));
+        CK(cudaMemset(eng->d_counters.p, 0, CNT_N * sizeof(unsigned long long)));
+        CK(cudaMemset(eng->d_error.p, 0, 2 * sizeof(int)));
+        return 0;
+    };
+    int rc = h->cfg.precision == 32 ? reset((Engine<float> *)h->eng.get()) : reset((Engine<double> *)h->eng.get());
+    if (rc) return rc;
+    h->nhist = 0; h->nbatch = 0;
+    return 0;
+}
+
+int egsgpu_get_tallies(egsgpu_handle *h, double *sum, double *sum2, double *totals) {
+    if (!h || !h->have_geom) return EGSGPU_ERR_STATE;
+    if (h->cfg.precision == 32) return get_tallies_impl(h, (Engine<float> *)h->eng.get(), sum, sum2, totals);
+    return get_tallies_impl(h, (Engine<double> *)h->eng.get(), sum, sum2, totals);
+}
+
+int egsgpu_get_dose(egsgpu_handle *h, double *dose, double *sigma) {
+    if (!h || !h->have_geom || !dose) return EGSGPU_ERR_ARG;
+    long long nv = (long long)h->nx * h->ny * h->nz;
+    std::vector<double> s(nv), s2(nv);
+    int rc = egsgpu_get_tallies(h, s.data(), s2.data(), nullptr);
+    if (rc) return rc;
+    const double N = (double)h->nhist, nb = (double)h->nbatch;
+    for (long long i = 0; i < nv; ++i) {
+        int iz = (int)(i / ((long long)h->nx * h->ny)), rr = (int)(i - (long long)iz * h->nx * h->ny);
+        int iy = rr / h->nx, ix = rr - iy * h->nx;
+        double vol = (h->xb[ix + 1] - h->xb[ix]) * (h->yb[iy + 1] - h->yb[iy]) * (h->zb[iz + 1] - h->zb[iz]);
+        double mass = vol * h->rhor[i] * h->H.media[h->med[i]].rho;
+        double norm = N > 0 ? 1.602e-10 / (mass * N) : 0;   // egs_dose_scoring.cpp:318-319
+        dose[i] = s[i] * norm;
+        if (sigma) {
+            // batch method: sigma of the mean of nb batch totals
+            double mean = s[i] / nb, var = nb > 1 ? (s2[i] / nb - mean * mean) / (nb - 1) : 0;
+            sigma[i] = (var > 0 ? std::sqrt(var) * nb : 0) * norm;
+        }
+    }
+    return 0;
+}
+
+int egsgpu_set_history_tally(egsgpu_handle *h, long long first, long long n) {
+    if (!h || n < 0 || n > (1LL << 24)) return EGSGPU_ERR_ARG;
+    std::string &err = h->err;
+    auto set = [&](auto *eng) -> int {
+        eng->hist_first = first;
+        eng->hist_n = n;
+        if (n > 0) {
+            CK(eng->d_hist.alloc(n * sizeof(double)));
+            CK(cudaMemset(eng->d_hist.p, 0, n * sizeof(double)));
+        }
+        return 0;
+    };
+    return h->cfg.precision == 32 ? set((Engine<float> *)h->eng.get()) : set((Engine<double> *)h->eng.get());
+}
+
+int egsgpu_get_history_tally(egsgpu_handle *h, double *out) {
+    if (!h || !out) return EGSGPU_ERR_ARG;
+    std::string &err = h->err;
+    auto get = [&](auto *eng) -> int {
+        if (eng->hist_n > 0) CK(cudaMemcpy(out, eng->d_hist.p, eng->hist_n * sizeof(double), cudaMemcpyDeviceToHost));
+        return 0;
+    };
+    return h->cfg.precision == 32 ? get((Engine<float> *)h->eng.get()) : get((Engine<double> *)h->eng.get());
+}
+
+// Checkpoint layout: magic, nvox, nhist, nbatch, energy[2], counters[8], sum[nvox], sum2[nvox]
+int egsgpu_checkpoint(egsgpu_handle *h, void *buf, size_t *size) {
+    if (!h || !size || !h->have_geom) return EGSGPU_ERR_ARG;
+    long long nv = (long long)h->nx * h->ny * h->nz;
+    size_t need = 8 * 4 + 2 * 8 + 8 * 8 + 2 * nv * 8;
+    if (!buf) { *size = need; return 0; }
+    if (*size < need) { *size = need; h->err = "checkpoint buffer too small"; return EGSGPU_ERR_ARG; }
+    std::string &err = h->err;
+    char *b = (char *)buf;
+    long long hdr[4] = {0x45475347505531LL, nv, h->nhist, h->nbatch};
+    std::memcpy(b, hdr, 32);
+    auto dump = [&](auto *eng) -> int {
+        CK(cudaMemcpy(b + 32, eng->d_energy.p, 16, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(b + 48, eng->d_counters.p, 64, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(b + 112, eng->d_sum.p, nv * 8, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(b + 112 + nv * 8, eng->d_sum2.p, nv * 8, cudaMemcpyDeviceToHost));
+        return 0;
+    };
+    *size = need;
+    return h->cfg.precision == 32 ? dump((Engine<float> *)h->eng.get()) : dump((Engine<double> *)h->eng.get());
+}
+
+int egsgpu_restore(egsgpu_handle *h, const void *buf, size_t size) {
+    if (!h || !buf || !h->have_geom) return EGSGPU_ERR_ARG;
+    long long nv = (long long)h->nx * h->ny * h->nz;
+    size_t need = 8 * 4 + 2 * 8 + 8 * 8 + 2 * nv * 8;
+    const char *b = (const char *)buf;
+    long long hdr[4];
+    if (size < need) { h->err = "checkpoint too small"; return EGSGPU_ERR_ARG; }
+    std::memcpy(hdr, b, 32);
+    if (hdr[0] != 0x45475347505531LL || hdr[1] != nv) { h->err = "checkpoint does not match this geometry"; return EGSGPU_ERR_ARG; }
+    std::string &err = h->err;
+    auto load = [&](auto *eng) -> int {
+        CK(cudaMemcpy(eng->d_energy.p, b + 32, 16, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(eng->d_counters.p, b + 48, 64, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(eng->d_sum.p, b + 112, nv * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(eng->d_sum2.p, b + 112 + nv * 8, nv * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemset(eng->d_dose.p, 0, nv * 8));
+        return 0;
+    };
+    int rc = h->cfg.precision == 32 ? load((Engine<float> *)h->eng.get()) : load((Engine<double> *)h->eng.get());
+    if (rc) return rc;
+    h->nhist = hdr[2];
+    h->nbatch = (int)hdr[3];
+    return 0;
+}
+
+const char *egsgpu_last_error(egsgpu_handle *h) { return h ? h->err.c_str() : "null handle"; }
+
+void egsgpu_destroy(egsgpu_handle *h) { delete h; }
+
+}  // extern "C"

@@ -1,0 +1,126 @@
+"""ORACLE -- test infrastructure only: ctypes binding of the FP64 CPU oracle
+(oracle/egs_oracle.cpp).  Used by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py as the checker; never by the product path."""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+DATA_DIR = os.path.join(ROOT, "egsnrc_gb300", "data")
+PEGS_FILE = os.path.join(DATA_DIR, "521icru.pegs4dat")
+
+_L = None
+
+
+def lib():
+    global _L
+    if _L is None:
+        if not os.path.exists(LIB_PATH):
+            import subprocess
+            subprocess.run(["make", "-s"], cwd=HERE, check=True)
+        L = C.CDLL(LIB_PATH)
+        vp, dp, i64 = C.c_void_p, C.POINTER(C.c_double), C.c_longlong
+        L.oracle_create.restype = vp
+        L.oracle_create.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(C.c_char_p), C.c_int, C.c_double, C.c_double]
+        L.oracle_destroy.argtypes = [vp]
+        L.oracle_set_geometry.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp, dp, dp, C.POINTER(C.c_int32), dp]
+        L.oracle_set_source.argtypes = [vp, C.c_void_p]
+        L.oracle_run.argtypes = [vp, i64, i64, C.c_int, C.c_uint32, C.c_int, C.c_int]
+        L.oracle_set_history_tally.argtypes = [vp, i64, i64]
+        L.oracle_get_history_tally.argtypes = [vp, dp]
+        L.oracle_get_tallies.argtypes = [vp, dp, dp, dp]
+        L.oracle_philox.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        L.oracle_ranmar.argtypes = [C.c_int, C.c_int, i64, dp]
+        L.oracle_child_sid.restype = C.c_uint64
+        L.oracle_child_sid.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32]
+        L.oracle_kn_sigma0.restype = C.c_double
+        L.oracle_kn_sigma0.argtypes = [C.c_double]
+        L.oracle_photon_xsec.argtypes = [vp, C.c_int, C.c_double, dp]
+        L.oracle_electron_xsec.argtypes = [vp, C.c_int, C.c_double, dp]
+        _L = L
+    return _L
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Oracle:
+    def __init__(self, media, ecut=0.521, pcut=0.010):
+        L = lib()
+        names = (C.c_char_p * len(media))(*[m.encode() for m in media])
+        h = L.oracle_create(DATA_DIR.encode(), PEGS_FILE.encode(), names, len(media), ecut, pcut)
+        if not h:
+            raise RuntimeError("oracle: media load failed")
+        self.h = C.c_void_p(h)
+        self.L = L
+        self.geom = None
+
+    def set_geometry(self, g):
+        self.geom = g
+        rc = self.L.oracle_set_geometry(self.h, g.nx, g.ny, g.nz, _dp(g.xb), _dp(g.yb), _dp(g.zb),
+                                        g.med.ctypes.data_as(C.POINTER(C.c_int32)), _dp(g.rhor))
+        if rc:
+            raise RuntimeError("oracle: bad geometry")
+
+    def set_source(self, src):
+        self.src = src
+        self.L.oracle_set_source(self.h, C.byref(src.s))
+
+    def run(self, n, nbatch=10, seed=1, first=0, ranmar=False, threads=1):
+        rc = self.L.oracle_run(self.h, int(first), int(n), int(nbatch), int(seed), int(bool(ranmar)), int(threads))
+        if rc:
+            raise RuntimeError("oracle run error %d" % rc)
+
+    def tallies(self):
+        nv = self.geom.nvox
+        s, s2, t = np.zeros(nv), np.zeros(nv), np.zeros(8)
+        self.L.oracle_get_tallies(self.h, _dp(s), _dp(s2), _dp(t))
+        return s, s2, t
+
+    def set_history_tally(self, first, n):
+        self._hist_n = n
+        self.L.oracle_set_history_tally(self.h, int(first), int(n))
+
+    def history_tally(self):
+        out = np.zeros(self._hist_n)
+        self.L.oracle_get_history_tally(self.h, _dp(out))
+        return out
+
+    def photon_xsec(self, med, e):
+        out = np.zeros(4)
+        self.L.oracle_photon_xsec(self.h, med, e, _dp(out))
+        return out
+
+    def electron_xsec(self, med, eke):
+        out = np.zeros(8)
+        self.L.oracle_electron_xsec(self.h, med, eke, _dp(out))
+        return out
+
+    def close(self):
+        if self.h:
+            self.L.oracle_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def philox(ctr, key):
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    lib().oracle_philox(c, k, o)
+    return list(o)
+
+
+def ranmar(n, ixx=0, jxx=0):
+    out = np.zeros(n)
+    lib().oracle_ranmar(ixx, jxx, n, _dp(out))
+    return out

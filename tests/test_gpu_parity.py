@@ -1,0 +1,180 @@
+"""GPU parity: the CUDA engine (through the C ABI) against the FP64 CPU oracle.
+
+Three levels, following the reference's lack of transport golden values:
+  * history by history: with Philox streams keyed by (seed, history) the FP64
+    GPU build and the oracle consume identical random numbers, so per-history
+    deposited energies agree to rounding except where a last-ulp difference in
+    a transcendental flips a rejection test;
+  * statistically: FP32 and FP64 voxel doses against the oracle inside the
+    combined 2-sigma band (expected coverage 95.4%; we require >= 93% of the
+    voxels above 20% of Dmax, >= 99% within 3 sigma, and the total deposited
+    energy within 3 sigma);
+  * exactly: energy conservation per run, and independence of the results
+    from the chunking of histories into wavefronts.
+"""
+import numpy as np
+import pytest
+
+import egsnrc_gb300 as eg
+from egsnrc_gb300 import workloads as W
+from oracle.oracle_binding import Oracle
+
+pytestmark = pytest.mark.gpu
+
+RM = eg.RM
+
+
+def make_pair(wl, precision=64, **cfg):
+    eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], precision=precision, **cfg)
+    eng.set_geometry(wl["geometry"])
+    eng.set_source(wl["source"])
+    ora = Oracle(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"])
+    ora.set_geometry(wl["geometry"])
+    ora.set_source(wl["source"])
+    return eng, ora
+
+
+def source_energy(src):
+    s = src.s
+    if s.spectrum:
+        return None
+    return s.energy + (2 * RM if s.charge > 0 else 0.0)
+
+
+def small_cases():
+    # reduced-size versions of the benchmark problems plus positron / bone cases
+    g = W.centred_geometry(20, 1.0)
+    yield "water_photon_2MeV", W.water30(20)
+    yield "slab_spectrum", dict(W.slab64(32), histories=0)
+    yield "water_electron_20MeV", dict(W.water128e(32), histories=0)
+    yield "perturbed_photon_6MeV", dict(W.perturbed64(24), histories=0)
+    yield "water_positron_5MeV", dict(name="pos", media=[W.WATER], ecut=0.521, pcut=0.01, geometry=g,
+                                      source=eg.ParallelBeam(charge=1, energy=5.0, position=(0.2, -0.3, -1.0)))
+    med = (np.arange(20 ** 3) % 4).astype(np.int32)
+    yield "mixed_media_electron", dict(name="mix", media=[W.WATER, W.LUNG, W.BONE, W.TISSUE], ecut=0.521,
+                                       pcut=0.01, geometry=W.centred_geometry(20, 0.5, med),
+                                       source=eg.ParallelBeam(charge=-1, energy=3.0, position=(0.1, 0.1, -1.0),
+                                                              direction=(0.1, 0.2, 1.0)))
+
+
+CASES = list(small_cases())
+NHIST = {"water_photon_2MeV": 3000, "slab_spectrum": 3000, "water_electron_20MeV": 300,
+         "perturbed_photon_6MeV": 2000, "water_positron_5MeV": 1000, "mixed_media_electron": 1000}
+
+
+@pytest.mark.parametrize("name,wl", CASES, ids=[c[0] for c in CASES])
+def test_history_by_history_fp64(name, wl):
+    n = NHIST[name]
+    eng, ora = make_pair(wl, precision=64)
+    eng.set_history_tally(0, n)
+    ora.set_history_tally(0, n)
+    eng.run(n, nbatch=2, seed=7)
+    ora.run(n, nbatch=2, seed=7)
+    hg, ho = eng.history_tally(), ora.history_tally()
+    rel = np.abs(hg - ho) / np.maximum(1e-12, np.abs(ho))
+    match = np.mean(rel < 1e-6)
+    assert match >= 0.97, "only %.3f of histories agree to 1e-6 (%s)" % (match, name)
+    # totals: deposited + escaped conserve the source energy
+    t = eng.totals()
+    e0 = source_energy(wl["source"])
+    if e0 is not None:
+        assert abs(t["deposited"] + t["escaped"] - n * e0) < 1e-8 * n * e0
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+@pytest.mark.parametrize("name", ["water_photon_2MeV", "water_electron_20MeV", "slab_spectrum"])
+def test_statistical_dose_band(name, precision):
+    wl = dict(CASES)[name]
+    n_gpu = {"water_photon_2MeV": 400000, "water_electron_20MeV": 40000, "slab_spectrum": 400000}[name]
+    n_ora = n_gpu // 4
+    eng, ora = make_pair(wl, precision=precision)
+    eng.run(n_gpu, nbatch=10, seed=11)
+    ora.run(n_ora, nbatch=10, seed=12, threads=8)
+    sg, s2g, tg = eng.tallies()
+    so, s2o, to = ora.tallies()
+
+    def mean_sigma(s, s2, nb, n):
+        m = s / nb
+        var = np.maximum(s2 / nb - m * m, 0) / (nb - 1)
+        return s / n, np.sqrt(var) * nb / n   # per-history mean and its sigma
+
+    dg, eg_ = mean_sigma(sg, s2g, 10, n_gpu)
+    do, eo = mean_sigma(so, s2o, 10, n_ora)
+    dmax = max(dg.max(), do.max())
+    sel = (do > 0.2 * dmax)
+    assert sel.sum() > 20
+    z = np.abs(dg[sel] - do[sel]) / np.sqrt(eg_[sel] ** 2 + eo[sel] ** 2 + 1e-300)
+    frac2, frac3 = np.mean(z < 2), np.mean(z < 3)
+    assert frac2 >= 0.93 and frac3 >= 0.99, (name, precision, frac2, frac3)
+    # total deposited energy per history
+    Eg, Eo = tg[2] / n_gpu, to[2] / n_ora
+    # batch estimate of the sigma of the total
+    sig = np.sqrt(np.sum(eg_ ** 2) + np.sum(eo ** 2))
+    assert abs(Eg - Eo) < 3 * max(sig, 1e-3 * Eo), (name, precision, Eg, Eo, sig)
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_energy_conservation(precision):
+    wl = W.water128e(32)
+    eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"], precision=precision)
+    eng.set_geometry(wl["geometry"])
+    eng.set_source(wl["source"])
+    n = 2000
+    eng.run(n, nbatch=4, seed=5)
+    t = eng.totals()
+    e0 = 20.0
+    tol = 1e-9 if precision == 64 else 2e-4
+    assert abs(t["deposited"] + t["escaped"] - n * e0) < tol * n * e0
+    s, _, _ = eng.tallies()
+    assert abs(s.sum() - t["deposited"]) < 1e-9 * t["deposited"]
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_chunking_invariance(precision):
+    wl = W.water30(20)
+    n = 5000
+    res = []
+    for chunk in (0, 333):
+        eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"], precision=precision, chunk=chunk)
+        eng.set_geometry(wl["geometry"])
+        eng.set_source(wl["source"])
+        eng.set_history_tally(0, n)
+        eng.run(n, nbatch=1, seed=3)
+        res.append(eng.history_tally())
+    # same streams, same arithmetic: identical per-history results
+    assert np.array_equal(res[0], res[1])
+
+
+def test_checkpoint_restore_roundtrip():
+    wl = W.water30(10)
+    eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"])
+    eng.set_geometry(wl["geometry"])
+    eng.set_source(wl["source"])
+    eng.run(2000, nbatch=2, seed=1)
+    blob = eng.checkpoint()
+    s1, q1, t1 = eng.tallies()
+    eng.run(2000, nbatch=2, seed=1, first=2000)
+    eng.restore(blob)
+    s2, q2, t2 = eng.tallies()
+    assert np.array_equal(s1, s2) and np.array_equal(q1, q2)
+    assert t1[0] == t2[0]
+    # resume: continuing from the checkpoint equals one uninterrupted run
+    eng.run(2000, nbatch=2, seed=1, first=2000)
+    ref = eg.DoseEngine(wl["media"], ecut=wl["ecut"])
+    ref.set_geometry(wl["geometry"])
+    ref.set_source(wl["source"])
+    ref.run(2000, nbatch=2, seed=1)
+    ref.run(2000, nbatch=2, seed=1, first=2000)
+    a, _, _ = eng.tallies()
+    b, _, _ = ref.tallies()
+    assert np.allclose(a, b, rtol=1e-12, atol=0)
+
+
+def test_capacity_error_is_reported():
+    wl = W.water30(10)
+    eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"], capacity=64, chunk=1000)
+    eng.set_geometry(wl["geometry"])
+    eng.set_source(wl["source"])
+    with pytest.raises(eg.EGSError) as ei:
+        eng.run(1000, nbatch=1, seed=1)
+    assert ei.value.code == 5

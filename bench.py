@@ -1,0 +1,348 @@
+"""Benchmark: histories/s and dose efficiency 1/(sigma^2 T) of the GB300
+transport engine on the heterogeneous slab phantom (64^3 x 0.25 cm, water /
+lung / bone / water, 10x10 cm photon field with a 0.1-6 MeV bremsstrahlung-like
+spectrum), one batch of 1e7 histories per step.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Prints one JSON line.  A step is one statistical batch of histories transported
+to completion; inputs (phantom, tables) are resident on the device for
+`value`; `e2e` repeats the step through the C ABI with host buffers (phantom
+upload and tally read-back inside the timed region).  Under torchrun every
+rank transports its own history range (weak scaling, no collective on the
+data path).  `--impl reference` times the CPU implementation of the same
+transport (the FP64 restatement of EGSnrc's PHOTON/ELECTR loop) on the host
+cores instead.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ALG_BYTES_PER_STEP = 104      # particle record read + write (48 + 48) + one FP64 tally update
+ALG_BYTES_PER_PUSH = 48       # one secondary record written to a queue
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="slab64")
+    ap.add_argument("--histories", type=float, default=1e7, help="histories per step (one batch)")
+    ap.add_argument("--precision", type=int, default=32)
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison leg")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--capacity", type=int, default=0, help="particle-queue capacity (0 = engine default)")
+    ap.add_argument("--chunk", type=int, default=0, help="histories per wavefront chunk (0 = automatic)")
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        if args.impl == "ours":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+        return ws, rank, local, dist
+    return 1, 0, 0, None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                      "--format=csv,noheader,nounits"], stdout=subprocess.PIPE,
+                                     stderr=subprocess.DEVNULL, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 3 + i and
+                          s[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return d.get(kernel)
+    except Exception:
+        return None
+
+
+def sigma_eff(sum_, sum2, nb, frac=0.5):
+    m = sum_ / nb
+    var = np.maximum(sum2 / nb - m * m, 0) / max(nb - 1, 1)
+    dose = sum_
+    sel = dose > frac * dose.max()
+    rel = np.sqrt(var[sel]) * nb / np.maximum(sum_[sel], 1e-300)
+    return float(np.sqrt(np.mean(rel * rel))), int(sel.sum())
+
+
+def cpu_sample(wl, seconds, threads, first):
+    """Times the CPU oracle on a bounded sample of the workload (rank 0, N = 1)."""
+    from oracle.oracle_binding import Oracle
+    ora = Oracle(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"])
+    ora.set_geometry(wl["geometry"])
+    ora.set_source(wl["source"])
+    n0 = 400 * threads
+    t0 = time.perf_counter()
+    ora.run(n0, nbatch=1, seed=wl["seed"], first=first, threads=threads)
+    dt0 = time.perf_counter() - t0
+    n = max(threads, int(n0 * max(seconds - dt0, 0.5) / max(dt0, 1e-3)))
+    t1 = time.perf_counter()
+    ora.run(n, nbatch=1, seed=wl["seed"], first=first + n0, threads=threads)
+    dt = time.perf_counter() - t1
+    return n, dt
+
+
+def reference_arm(args, wl, ws, rank, dist):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    K, W = args.steps, args.warmup
+    # size one step to about 4 s of host work
+    from oracle.oracle_binding import Oracle
+    ora = Oracle(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"])
+    ora.set_geometry(wl["geometry"])
+    ora.set_source(wl["source"])
+    n0 = 200 * threads
+    t0 = time.perf_counter()
+    ora.run(n0, nbatch=1, seed=wl["seed"], first=0, threads=threads)
+    rate = n0 / max(time.perf_counter() - t0, 1e-3)
+    per_step = max(threads, int(rate * 4.0))
+    first = n0
+    for _ in range(W):
+        ora.run(per_step, nbatch=1, seed=wl["seed"], first=first, threads=threads)
+        first += per_step
+    ora2 = Oracle(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"])
+    ora2.set_geometry(wl["geometry"])
+    ora2.set_source(wl["source"])
+    t0 = time.perf_counter()
+    for _ in range(K):
+        ora2.run(per_step, nbatch=1, seed=wl["seed"], first=first, threads=threads)
+        first += per_step
+    T = time.perf_counter() - t0
+    value = per_step * K / T
+    s, s2, tot = ora2.tallies()
+    sig, nsel = sigma_eff(s, s2, K) if K > 1 else (None, 0)
+    eff = (1.0 / (sig * sig * T)) if sig else None
+    line = {"impl": "reference", "metric": "histories_per_second", "value": value, "unit": "histories/s",
+            "n_gpus": args.gpus, "steps": K, "warmup": W, "ms_per_step": 1e3 * T / K,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config_of(wl, per_step),
+            "dose_efficiency": eff, "sigma_bar_50pct": sig,
+            "cpu_baseline": {"value": value, "unit": "histories/s", "cores": threads, "kind": "port",
+                             "sample": "%d histories per step x %d steps of %s (FP64 CPU restatement of the "
+                                       "reference transport, one thread per core)" % (per_step, K, wl["name"])},
+            "e2e": {"value": value, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_of(wl, per_step):
+    g = wl["geometry"]
+    return {"workload": wl["name"], "phantom": "%dx%dx%d voxels" % (g.nx, g.ny, g.nz),
+            "media": wl["media"], "histories_per_step": int(per_step), "batches_per_step": 1,
+            "ecut_MeV": wl["ecut"], "pcut_MeV": wl["pcut"],
+            "l2": "256 MiB buffer written between timed steps"}
+
+
+def main():
+    args = parse()
+    from egsnrc_gb300 import workloads as W
+    wl = W.WORKLOADS[args.workload]()
+    ws, rank, local, dist = dist_setup(args)
+    if args.impl == "reference":
+        reference_arm(args, wl, ws, rank, dist)
+        if dist:
+            dist.barrier()
+        return
+    import torch
+    import egsnrc_gb300 as eg
+    torch.cuda.set_device(local)
+    H = int(args.histories)
+    K, Wm = args.steps, args.warmup
+    ekw = dict(capacity=args.capacity, chunk=args.chunk)
+    eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], precision=args.precision, **ekw)
+    eng.set_geometry(wl["geometry"])
+    eng.set_source(wl["source"])
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    base = rank * (K + Wm + 2) * H     # disjoint history ranges per rank
+    first = base
+    for _ in range(Wm):
+        eng.run(H, nbatch=1, seed=wl["seed"], first=first)
+        first += H
+    eng.reset()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        start.record()
+        for _ in range(K):
+            flush.zero_()
+            eng.run(H, nbatch=1, seed=wl["seed"], first=first)
+            first += H
+        stop.record()
+        torch.cuda.synchronize()
+        t_host = time.perf_counter() - t0
+    T = start.elapsed_time(stop) / 1e3
+    if dist:
+        tt = torch.tensor([T], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        T = float(tt.item())
+    prof = eng.profile()
+    s, s2, tot = eng.tallies()
+    sig, nsel = sigma_eff(s, s2, K) if K > 1 else (None, 0)
+    value = H * ws * K / T
+    eff = (1.0 / (sig * sig * T)) if sig else None
+
+    # roofline of the dominant kernel: algorithmic bytes / CUDA-event kernel time
+    kern = "electron" if prof["ms_electron"] >= prof["ms_photon"] else "photon"
+    steps_k = prof[kern + "_steps"]
+    pushes_k = prof[kern + "_pushes"]
+    ms_k, n_k = prof["ms_" + kern], max(prof["launches_" + kern], 1)
+    bytes_k = steps_k * ALG_BYTES_PER_STEP + pushes_k * ALG_BYTES_PER_PUSH
+    achieved = bytes_k / (ms_k / 1e3) / 1e9 if ms_k > 0 else None
+    peak, peak_kind = measured_peak_hbm()
+    traffic = ncu_traffic("k_" + kern)
+    roof = {"bound": "hbm", "kernel": "k_" + kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
+            "traffic": traffic, "alg_bytes_per_launch": bytes_k / n_k, "launches": n_k,
+            "ms_per_launch": ms_k / n_k, "steps_per_s": steps_k / (ms_k / 1e3) if ms_k > 0 else None,
+            "kernel_share": {k: prof["ms_" + k] / max(1e-9, sum(prof["ms_" + j] for j in
+                                                                  ("source", "photon", "electron", "batch")))
+                             for k in ("source", "photon", "electron", "batch")}}
+    launches = sum(prof["launches_" + k] for k in ("source", "photon", "electron", "batch"))
+
+    # e2e through the C ABI with host buffers: phantom upload + run + tally read-back
+    g = wl["geometry"]
+    e2e_eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], precision=args.precision, **ekw)
+    e2e_eng.set_geometry(g)
+    e2e_eng.set_source(wl["source"])
+    h2d = g.xb.nbytes + g.yb.nbytes + g.zb.nbytes + g.med.nbytes + g.rhor.nbytes
+    d2h = 2 * g.nvox * 8 + 8 * 8
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    te0 = time.perf_counter()
+    for _ in range(K):
+        flush.zero_()
+        e2e_eng.set_geometry(g)
+        e2e_eng.run(H, nbatch=1, seed=wl["seed"], first=first)
+        first += H
+        ss, ss2, _ = e2e_eng.tallies()
+    torch.cuda.synchronize()
+    Te = time.perf_counter() - te0
+    if dist:
+        tt = torch.tensor([Te], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        Te = float(tt.item())
+    e2e = {"value": H * ws * K / Te, "unit": "histories/s", "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "path": "egsgpu_set_xyz_geometry + egsgpu_run + egsgpu_get_tallies"}
+
+    line = {"metric": "histories_per_second", "value": value, "unit": "histories/s", "n_gpus": ws, "steps": K,
+            "warmup": Wm, "ms_per_step": 1e3 * T / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if args.precision == 32 else "f64", "data": "synthetic",
+            "config": config_of(wl, H), "dose_efficiency": eff, "dose_efficiency_unit": "1/(sigma^2 s)",
+            "sigma_bar_50pct": sig, "voxels_above_50pct": nsel, "e2e": e2e, "roofline": roof,
+            "gpu_launches": int(launches), "host_seconds": t_host}
+
+    if rank == 0 and not args.no_fp64 and args.precision == 32:
+        # plain FP64 GPU form on the same problem: histories/s and efficiency
+        e64 = eg.DoseEngine(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], precision=64, **ekw)
+        e64.set_geometry(g)
+        e64.set_source(wl["source"])
+        H64 = max(H // 10, 100000)
+        e64.run(H64 // 4, nbatch=1, seed=wl["seed"], first=first)
+        e64.reset()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(4):
+            e64.run(H64, nbatch=1, seed=wl["seed"], first=first)
+            first += H64
+        torch.cuda.synchronize()
+        T64 = time.perf_counter() - t0
+        s64, s264, _ = e64.tallies()
+        sig64, _ = sigma_eff(s64, s264, 4)
+        eff64 = 1.0 / (sig64 * sig64 * T64) if sig64 else None
+        line["fp64"] = {"value": 4 * H64 / T64, "unit": "histories/s", "dose_efficiency": eff64,
+                        "histories_per_step": H64, "steps": 4}
+        if eff and eff64:
+            line["efficiency_ratio_fp32_over_fp64"] = eff / eff64
+    line["clocks"] = clk.summary()
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        n, dt = cpu_sample(wl, args.cpu_seconds, threads, first + 10 ** 8)
+        line["cpu_baseline"] = {"value": n / dt, "unit": "histories/s", "cores": threads, "kind": "port",
+                                "sample": "%d histories of %s on %d host threads, %.1f s" % (n, wl["name"],
+                                                                                          threads, dt)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

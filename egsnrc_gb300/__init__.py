@@ -67,6 +67,7 @@ def load_library():
     L.egsgpu_reset.argtypes = [vp]
     L.egsgpu_get_tallies.argtypes = [vp, dp, dp, dp]
     L.egsgpu_get_dose.argtypes = [vp, dp, dp]
+    L.egsgpu_get_profile.argtypes = [vp, dp]
     L.egsgpu_set_history_tally.argtypes = [vp, i64, i64]
     L.egsgpu_get_history_tally.argtypes = [vp, dp]
     L.egsgpu_checkpoint.argtypes = [vp, vp, C.POINTER(C.c_size_t)]
@@ -201,6 +202,16 @@ class DoseEngine:
         d, s = np.zeros(nv), np.zeros(nv)
         self._check(self.L.egsgpu_get_dose(self.h, _dp(d), _dp(s)))
         return d, s
+
+    def profile(self):
+        o = np.zeros(14)
+        self._check(self.L.egsgpu_get_profile(self.h, _dp(o)))
+        keys = ("source", "photon", "electron", "batch")
+        d = {"ms_" + k: o[i] for i, k in enumerate(keys)}
+        d.update({"launches_" + k: int(o[4 + i]) for i, k in enumerate(keys)})
+        d.update(photon_steps=o[8], electron_steps=o[9], photon_pushes=o[10], electron_pushes=o[11],
+                 photon_interactions=o[12], electron_interactions=o[13])
+        return d
 
     def set_history_tally(self, first, n):
         self._hist_n = n

@@ -16,7 +16,6 @@ constexpr int MS_NL = 64, MS_NQ = 8, MS_NU = 32;
 constexpr int MAXMED = 16;            // media per problem (constant-memory scalars)
 constexpr int MAXNE = 12;             // elements per medium
 constexpr int LOOP_CAP = 100000;      // cap on every rejection loop
-typedef double RT;                    // residual range / energy loss type
 
 // ------------------------------------------------------------- tables ----
 // Per-medium scalars, one struct per medium in constant memory.
@@ -26,7 +25,7 @@ struct MedScalars {
         zbrang, lzbrang;
     Real dl[6][8];
     Real bpar[2];
-    RT E_array0;
+    Real E_array0;
     int meke, n_shell, nne, sig_mono_e, sig_mono_p;
     int etab_off, gtab_off, shell_off, elem_off;
     float pz[MAXNE];
@@ -37,7 +36,7 @@ template <class Real>
 struct Tables {
     const Real *etab;     // [medium][meke][16]: esig0,esig1,psig0,psig1,ededx0,ededx1,pdedx0,pdedx1,
                           //                     ebr10,ebr11,pbr10,pbr11,pbr20,pbr21,tmxs0,tmxs1
-    const RT *erange;     // [medium][meke][4]: E_array, range_ep0, range_ep1, pad
+    const Real *erange;   // [medium][meke][4]: E_array, range_ep0, range_ep1, pad
     const Real *gtab;     // [medium][MXGE][8]: gmfp0,gmfp1,gbr10,gbr11,gbr20,gbr21,cohe0,cohe1
     const Real *pmax;     // [medium][MXGE][2]
     const Real *ray;      // [medium][4][NRAY]: xgrid, fcum, b_array, c_array
@@ -141,9 +140,11 @@ template <class Real>
 __device__ inline Real urand(Rng &r) { return (Real)r.u(); }
 
 // --------------------------------------------------------- math shims ----
-__device__ inline float dlog(float x) { return logf(x); }
+// FP32 transport uses the SFU-based intrinsics; FP64 uses the full-precision
+// library functions (so that the FP64 build tracks the CPU oracle).
+__device__ inline float dlog(float x) { return __logf(x); }
 __device__ inline double dlog(double x) { return log(x); }
-__device__ inline float dexp(float x) { return expf(x); }
+__device__ inline float dexp(float x) { return __expf(x); }
 __device__ inline double dexp(double x) { return exp(x); }
 __device__ inline float dsqrt(float x) { return sqrtf(x); }
 __device__ inline double dsqrt(double x) { return sqrt(x); }

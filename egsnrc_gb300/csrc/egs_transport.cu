@@ -48,7 +48,7 @@ template <> __device__ inline const MedScalars<double> &cmed<double>(int m) { re
 // (EGSGPU_ERR_LOOP); no physical history comes near it.
 constexpr int STEP_CAP = 1 << 22;
 
-enum { CNT_PSTEP = 0, CNT_ESTEP = 1, CNT_PUSH = 2, CNT_INTER = 3, CNT_N = 8 };
+enum { CNT_PSTEP = 0, CNT_ESTEP = 1, CNT_PUSH = 2, CNT_INTER = 3, CNT_EPUSH = 4, CNT_EINTER = 5, CNT_N = 8 };
 
 template <class Real>
 struct Params {
@@ -65,26 +65,27 @@ struct Params {
 };
 
 // ------------------------------------------------------------- tallies ----
+template <class Real>
 struct Acc {
     int ir;
     uint32_t hist;
-    double e;
+    Real e;   // deposits of one particle's visit to one voxel
 };
 
 template <class Real>
-__device__ inline void acc_flush(const Params<Real> &P, Acc &a) {
+__device__ inline void acc_flush(const Params<Real> &P, Acc<Real> &a) {
     if (a.ir >= 0 && a.e > 0) {
-        atomicAdd(P.dose + a.ir, a.e);
+        atomicAdd(P.dose + a.ir, (double)a.e);
         if (P.hist_tally) {
             long long i = (long long)a.hist - P.hist_first;
-            if (i >= 0 && i < P.hist_n) atomicAdd(P.hist_tally + i, a.e);
+            if (i >= 0 && i < P.hist_n) atomicAdd(P.hist_tally + i, (double)a.e);
         }
     }
     a.e = 0;
     a.ir = -1;
 }
 template <class Real>
-__device__ inline void deposit(const Params<Real> &P, Acc &a, int ir, uint32_t hist, double e) {
+__device__ inline void deposit(const Params<Real> &P, Acc<Real> &a, int ir, uint32_t hist, Real e) {
     if (ir < 0 || !(e > 0)) return;
     if (ir != a.ir || hist != a.hist) {
         acc_flush(P, a);
@@ -266,7 +267,7 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
     (void)s_dummy;
     Particle<Real> p;
     PhotonState<Real> s;
-    Acc acc{-1, 0u, 0.0};
+    Acc<Real> acc{-1, 0u, (Real)0};
     bool alive = false, exhausted = false;
     unsigned long long nstep = 0, npush = 0, ninter = 0;
     double edep_tot = 0, esc_tot = 0;
@@ -294,7 +295,7 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
 
         if (s.state == 0) {   // :PNEWENERGY:
             if (p.E <= T.pcut) {   // :PCUT-DISCARD:
-                deposit(P, acc, p.ir, p.rng.hist, (double)(p.E * p.wt));
+                deposit(P, acc, p.ir, p.rng.hist, p.E * p.wt);
                 edep_tot += (double)(p.E * p.wt);
                 alive = false;
                 continue;
@@ -365,13 +366,13 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
             Real edep = compton(T, M, p, e.u, e.v, e.w, e.E, err);
             e.iq = -1;
             e.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
-            if (edep > 0) { deposit(P, acc, p.ir, p.rng.hist, (double)(edep * p.wt)); edep_tot += (double)(edep * p.wt); }
+            if (edep > 0) { deposit(P, acc, p.ir, p.rng.hist, edep * p.wt); edep_tot += (double)(edep * p.wt); }
             q_push(P, P.ein, e, npush);
             s.state = 0;
             continue;
         }
         Real edep = photo(T, M, p, s.gle, err);
-        if (edep > 0) { deposit(P, acc, p.ir, p.rng.hist, (double)(edep * p.wt)); edep_tot += (double)(edep * p.wt); }
+        if (edep > 0) { deposit(P, acc, p.ir, p.rng.hist, edep * p.wt); edep_tot += (double)(edep * p.wt); }
         q_push(P, P.ein, p, npush);
         alive = false;
     }
@@ -400,7 +401,7 @@ struct ElecState {
     int state;            // 0 new electron, 1 new tstep, 2 ustep
     int medium, lelke, compute_tstep, nsteps;
     Real rhor, eke, elke, sig0, demfp;
-    RT total_de, total_tstep;
+    Real total_de, total_tstep;
 };
 
 // Electron-table row accessor: 16 coefficients per energy bin.
@@ -418,49 +419,49 @@ __device__ inline const Real *erow(const Tables<Real> &T, const MedScalars<Real>
     return T.etab + ((size_t)M.etab_off + lel - 1) * 16;
 }
 template <class Real>
-__device__ inline const RT *rrow(const Tables<Real> &T, const MedScalars<Real> &M, int lel) {
+__device__ inline const Real *rrow(const Tables<Real> &T, const MedScalars<Real> &M, int lel) {
     return T.erange + ((size_t)M.etab_off + lel - 1) * 4;
 }
 
 // $COMPUTE-DRANGE (src/egsnrc.macros:3214-3238)
 template <class Real>
-__device__ inline RT drange(const Tables<Real> &T, const MedScalars<Real> &M, int qel, RT e1, RT e2, int lel,
-                            RT el1, RT el2) {
+__device__ inline Real drange(const Tables<Real> &T, const MedScalars<Real> &M, int qel, Real e1, Real e2, int lel,
+                            Real el1, Real el2) {
     const Real *r = erow(T, M, lel);
-    RT fedep = 1 - e2 / e1;
-    RT elktmp = 0.5 * (el1 + el2 + 0.25 * fedep * fedep * (1 + fedep * (1 + 0.875 * fedep)));
-    RT d0 = qel ? (RT)r[6] : (RT)r[4], d1 = qel ? (RT)r[7] : (RT)r[5];
-    RT dedxmid = 1 / (d1 * elktmp + d0);
-    RT aux = d1 * dedxmid;
+    Real fedep = 1 - e2 / e1;
+    Real elktmp = 0.5 * (el1 + el2 + 0.25 * fedep * fedep * (1 + fedep * (1 + 0.875 * fedep)));
+    Real d0 = qel ? (Real)r[6] : (Real)r[4], d1 = qel ? (Real)r[7] : (Real)r[5];
+    Real dedxmid = 1 / (d1 * elktmp + d0);
+    Real aux = d1 * dedxmid;
     aux = aux * (1 + 2 * aux) * (fedep / (2 - fedep)) * (fedep / (2 - fedep)) / 6;
     return fedep * e1 * dedxmid * (1 + aux);
 }
 // $COMPUTE-ELOSS (:3290-3312)
 template <class Real>
-__device__ inline RT eloss(const Tables<Real> &T, const MedScalars<Real> &M, int qel, RT step, RT eke, RT elke,
-                           int lel, RT rhof) {
+__device__ inline Real eloss(const Tables<Real> &T, const MedScalars<Real> &M, int qel, Real step, Real eke, Real elke,
+                           int lel, Real rhof) {
     const Real *r = erow(T, M, lel);
-    RT d0 = qel ? (RT)r[6] : (RT)r[4], d1 = qel ? (RT)r[7] : (RT)r[5];
-    RT dedxmid = d1 * elke + d0;
-    RT aux = d1 / dedxmid;
-    RT de = dedxmid * step * rhof;
-    RT fedep = de / eke;
+    Real d0 = qel ? (Real)r[6] : (Real)r[4], d1 = qel ? (Real)r[7] : (Real)r[5];
+    Real dedxmid = d1 * elke + d0;
+    Real aux = d1 / dedxmid;
+    Real de = dedxmid * step * rhof;
+    Real fedep = de / eke;
     return de * (1 - 0.5 * fedep * aux * (1 - 0.333333 * fedep * (aux - 1 - 0.25 * fedep * (2 - aux * (4 - aux)))));
 }
 // $COMPUTE-ELOSS-G (:3315-3351)
 template <class Real>
-__device__ inline RT eloss_g(const Tables<Real> &T, const MedScalars<Real> &M, int qel, RT step, RT eke, RT elke,
-                             int lel, RT range, RT rhof) {
-    RT tuss = range - rrow(T, M, lel)[1 + qel] / rhof;
+__device__ inline Real eloss_g(const Tables<Real> &T, const MedScalars<Real> &M, int qel, Real step, Real eke, Real elke,
+                             int lel, Real range, Real rhof) {
+    Real tuss = range - rrow(T, M, lel)[1 + qel] / rhof;
     if (tuss >= step) return eloss(T, M, qel, step, eke, elke, lel, rhof);
     int lt = lel;
     tuss = (range - step) * rhof;
-    if (tuss <= 0) return eke - (RT)M.te * 0.99;
+    if (tuss <= 0) return eke - (Real)M.te * 0.99;
     while (lt > 1 && tuss < rrow(T, M, lt)[1 + qel]) --lt;
     if (lt > M.meke - 1) lt = M.meke - 1;
-    RT elktmp = (lt + 1 - (RT)M.eke0) / (RT)M.eke1, eketmp = rrow(T, M, lt + 1)[0];
+    Real elktmp = (lt + 1 - (Real)M.eke0) / (Real)M.eke1, eketmp = rrow(T, M, lt + 1)[0];
     tuss = (rrow(T, M, lt + 1)[1 + qel] - tuss) / rhof;
-    RT de = eloss(T, M, qel, tuss, eketmp, elktmp, lt, rhof);
+    Real de = eloss(T, M, qel, tuss, eketmp, elktmp, lt, rhof);
     return de + eke - eketmp;
 }
 
@@ -472,7 +473,8 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
     const unsigned nq = *P.ein.count < P.ein.capacity ? *P.ein.count : P.ein.capacity;
     Particle<Real> p;
     ElecState<Real> s;
-    Acc acc{-1, 0u, 0.0};
+    Real edep_part = 0;   // continuous-loss deposits of the current particle
+    Acc<Real> acc{-1, 0u, (Real)0};
     bool alive = false, exhausted = false;
     unsigned long long nstep = 0, npush = 0, ninter = 0;
     double edep_tot = 0, esc_tot = 0;
@@ -486,6 +488,8 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
             base = __shfl_sync(0xffffffffu, base, __ffs(need) - 1);
             if (base >= nq) exhausted = true;
             if (!alive) {
+                edep_tot += (double)edep_part;
+                edep_part = 0;
                 unsigned idx = base + __popc(need & ((1u << lane) - 1u));
                 if (idx < nq) {
                     q_load(P.ein, idx, P.seed, p);
@@ -524,24 +528,24 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
             // :USTEP: one condensed-history step
             const MedScalars<Real> &M = cmed<Real>(s.medium);
             Real rhof = s.rhor, sig = s.sig0;
-            RT tstep;
-            const RT *rr = rrow(T, M, s.lelke);
+            Real tstep;
+            const Real *rr = rrow(T, M, s.lelke);
             if (sig <= 0) { tstep = 1e8; s.sig0 = (Real)1e-15; }
             else {
                 if (s.compute_tstep) {
-                    s.total_de = (RT)s.demfp / (RT)sig;
-                    RT eke = s.eke, elke = s.elke, ekef = eke - s.total_de;
+                    s.total_de = (Real)s.demfp / (Real)sig;
+                    Real eke = s.eke, elke = s.elke, ekef = eke - s.total_de;
                     if (ekef <= M.E_array0) tstep = 1e8;
                     else {
-                        RT elkef = log(ekef);
-                        int lelkef = min(max((int)((RT)M.eke1 * elkef + (RT)M.eke0), 1), s.lelke);
+                        Real elkef = dlog(ekef);
+                        int lelkef = min(max((int)((Real)M.eke1 * elkef + (Real)M.eke0), 1), s.lelke);
                         if (lelkef == s.lelke) tstep = drange(T, M, qel, eke, ekef, s.lelke, elke, elkef);
                         else {
-                            RT ekei = rr[0], elkei = (s.lelke - (RT)M.eke0) / (RT)M.eke1;
-                            RT tuss = drange(T, M, qel, eke, ekei, s.lelke, elke, elkei);
-                            const RT *rf = rrow(T, M, lelkef + 1);
+                            Real ekei = rr[0], elkei = (s.lelke - (Real)M.eke0) / (Real)M.eke1;
+                            Real tuss = drange(T, M, qel, eke, ekei, s.lelke, elke, elkei);
+                            const Real *rf = rrow(T, M, lelkef + 1);
                             ekei = rf[0];
-                            elkei = (lelkef + 1 - (RT)M.eke0) / (RT)M.eke1;
+                            elkei = (lelkef + 1 - (Real)M.eke0) / (Real)M.eke1;
                             tstep = drange(T, M, qel, ekei, ekef, lelkef, elkei, elkef);
                             tstep = tstep + tuss + rr[1 + qel] - rf[1 + qel];
                         }
@@ -549,20 +553,20 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                     s.total_tstep = tstep;
                     s.compute_tstep = 0;
                 }
-                tstep = s.total_tstep / (RT)rhof;
+                tstep = s.total_tstep / (Real)rhof;
             }
             ERow<Real> er{erow(T, M, s.lelke), qel};
             const Real *row = er.r;
             Real dedx0 = er.dedx(s.elke), dedx = rhof * dedx0;
             Real tmxs = (row[15] * s.elke + row[14]) / rhof;
-            RT range;
+            Real range;
             {
-                RT ekei = rr[0], elkei = (s.lelke - (RT)M.eke0) / (RT)M.eke1;
-                range = drange(T, M, qel, (RT)s.eke, ekei, s.lelke, (RT)s.elke, elkei);
-                range = (range + rr[1 + qel]) / (RT)rhof;
+                Real ekei = rr[0], elkei = (s.lelke - (Real)M.eke0) / (Real)M.eke1;
+                range = drange(T, M, qel, (Real)s.eke, ekei, s.lelke, (Real)s.elke, elkei);
+                range = (range + rr[1 + qel]) / (Real)rhof;
             }
             tmxs = dmin(tmxs, T.smaxir);
-            Real tustep = (Real)dmin(tstep, dmin((RT)tmxs, range));
+            Real tustep = (Real)dmin(tstep, dmin((Real)tmxs, range));
             Real tperp = hownear(G, p.ir, p.x, p.y, p.z);
             Real blccl = rhof * M.blcc;
             Real p2 = s.eke * (s.eke + 2 * rm), beta2 = p2 / (p2 + rm * rm);
@@ -570,12 +574,12 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
             tustep = dmin(tustep, dmax(tperp, skindepth));
             bool callhowfar, dosingle = false, callmsdist;
             Real ustep, uf, vf, wf, xf, yf, zf;
-            RT de = 0;
+            Real de = 0;
             ++nstep;
             if (tustep <= tperp && tustep > skindepth) {
                 callhowfar = false;
                 callmsdist = true;
-                de = eloss_g(T, M, qel, (RT)tustep, (RT)s.eke, (RT)s.elke, s.lelke, range, (RT)rhof);
+                de = eloss_g(T, M, qel, (Real)tustep, (Real)s.eke, (Real)s.elke, s.lelke, range, (Real)rhof);
                 msdist_pII(T, M, p, s.eke, (Real)de, tustep, rhof, uf, vf, wf, xf, yf, zf, err);
                 ustep = tustep;
             } else {
@@ -619,10 +623,10 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                 if (callhowfar) {
                     tvstep = vstep;
                     if (tvstep != tustep) dosingle = false;
-                    de = eloss_g(T, M, qel, (RT)tvstep, (RT)s.eke, (RT)s.elke, s.lelke, range, (RT)rhof);
+                    de = eloss_g(T, M, qel, (Real)tvstep, (Real)s.eke, (Real)s.elke, s.lelke, range, (Real)rhof);
                 } else {
                     tvstep = tustep;
-                    if (!callmsdist) de = eloss_g(T, M, qel, (RT)tvstep, (RT)s.eke, (RT)s.elke, s.lelke, range, (RT)rhof);
+                    if (!callmsdist) de = eloss_g(T, M, qel, (Real)tvstep, (Real)s.eke, (Real)s.elke, s.lelke, range, (Real)rhof);
                 }
                 Real edep = (Real)de, ekef = s.eke - edep;
                 if (!callmsdist) {
@@ -638,8 +642,8 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                         rotate(p.u, p.v, p.w, sinthe, costhe, az, uf, vf, wf);
                     } else { uf = p.u; vf = p.v; wf = p.w; }
                 }
-                deposit(P, acc, p.ir, p.rng.hist, (double)edep * (double)p.wt);   // AUSGAB(0)
-                edep_tot += (double)edep * (double)p.wt;
+                deposit(P, acc, p.ir, p.rng.hist, edep * p.wt);   // AUSGAB(0)
+                edep_part += edep * p.wt;
                 p.x = xf; p.y = yf; p.z = zf; p.u = uf; p.v = vf; p.w = wf;
                 p.E = p.E - edep;
                 if (irnew == p.ir && p.E <= T.ecut) ecut_discard = true;
@@ -662,9 +666,9 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                     else if (s.medium != medold) { s.state = 1; continue; }
                     else {
                         // $UPDATE-DEMFP (src/egsnrc.macros:3273-3281)
-                        s.demfp = s.demfp - (Real)(de * (RT)sig);
+                        s.demfp = s.demfp - (Real)(de * (Real)sig);
                         s.total_de = s.total_de - de;
-                        s.total_tstep = s.total_tstep - (RT)tvstep * (RT)rhof;
+                        s.total_tstep = s.total_tstep - (Real)tvstep * (Real)rhof;
                         if (s.total_tstep < 1e-9) s.demfp = 0;
                         if (!(s.demfp < (Real)1e-8)) continue;
                         // fictitious-cross-section rejection
@@ -868,7 +872,7 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
         // :ECUT-DISCARD: (src/egsnrc.mortran:1768-1802)
         {
             Real edep = p.E - rm;
-            deposit(P, acc, p.ir, p.rng.hist, (double)(edep * p.wt));
+            deposit(P, acc, p.ir, p.rng.hist, edep * p.wt);
             edep_tot += (double)(edep * p.wt);
             if (p.iq > 0) {   // ANNIH_AT_REST (src/egsnrc.mortran:186-223)
                 Real costhe = urand<Real>(p.rng);
@@ -886,6 +890,7 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
         }
     }
     acc_flush(P, acc);
+    edep_tot += (double)edep_part;
     for (int o = 16; o > 0; o >>= 1) {
         nstep += __shfl_down_sync(0xffffffffu, nstep, o);
         npush += __shfl_down_sync(0xffffffffu, npush, o);
@@ -895,8 +900,8 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
     }
     if (lane == 0) {
         atomicAdd(P.counters + CNT_ESTEP, nstep);
-        atomicAdd(P.counters + CNT_PUSH, npush);
-        atomicAdd(P.counters + CNT_INTER, ninter);
+        atomicAdd(P.counters + CNT_EPUSH, npush);
+        atomicAdd(P.counters + CNT_EINTER, ninter);
         atomicAdd(P.energy + 0, edep_tot);
         atomicAdd(P.energy + 1, esc_tot);
     }
@@ -973,18 +978,37 @@ struct Engine : EngineBase {
     DevMem d_dose, d_sum, d_sum2, d_energy, d_counters, d_error, d_hist;
     long long hist_first = 0, hist_n = 0;
     int sm_count = 0;
+    // per-kernel device time (CUDA events on the launch stream) and launches:
+    // 0 source, 1 photon, 2 electron, 3 batch
+    double prof_ms[4] = {0, 0, 0, 0};
+    long long prof_n[4] = {0, 0, 0, 0};
+    cudaEvent_t ev[8] = {};
+    bool events_ready = false;
+    long long tuned_chunk = 0;   // histories per wavefront chosen by the autotuner
 
     explicit Engine(const egsgpu_config &c) : cfg(c) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev);
     }
+    ~Engine() {
+        if (events_ready)
+            for (auto &e : ev) cudaEventDestroy(e);
+    }
+    // accumulate the elapsed time between events 2k and 2k+1 (after a sync)
+    void prof_take(int k, int slot) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, ev[2 * slot], ev[2 * slot + 1]) == cudaSuccess) {
+            prof_ms[k] += ms;
+            ++prof_n[k];
+        }
+    }
 
     int load(const egs::Hatch &H, double ecut, double pcut, double skindepth, std::string &err) override {
         nmed = (int)H.media.size();
         if (nmed > MAXMED) { err = "too many media"; return EGSGPU_ERR_ARG; }
         std::vector<Real> etab, gtab, pmax, ray, shell, elem, ms;
-        std::vector<RT> erange;
+        std::vector<Real> erange;
         std::vector<int> rayi, shellat, msi;
         meds.assign(nmed, MedScalars<Real>());
         int eoff = 0, goff = 0, soff = 0, loff = 0;
@@ -1000,7 +1024,7 @@ struct Engine : EngineBase {
             for (int k = 0; k < 6; ++k)
                 for (int l = 0; l < 8; ++l) M.dl[k][l] = (Real)m.dl[k][l];
             M.bpar[0] = (Real)m.bpar[0]; M.bpar[1] = (Real)m.bpar[1];
-            M.E_array0 = m.E_array[0];
+            M.E_array0 = (Real)m.E_array[0];
             M.meke = m.meke; M.n_shell = m.n_shell; M.nne = m.nne;
             M.sig_mono_e = m.sig_ismonotone[0]; M.sig_mono_p = m.sig_ismonotone[1];
             M.etab_off = eoff; M.gtab_off = goff; M.shell_off = soff; M.elem_off = loff;
@@ -1011,8 +1035,8 @@ struct Engine : EngineBase {
                                       m.pdedx0[i], m.pdedx1[i], m.ebr10[i], m.ebr11[i], m.pbr10[i], m.pbr11[i],
                                       m.pbr20[i], m.pbr21[i], m.tmxs0[i], m.tmxs1[i]};
                 for (double x : v) etab.push_back((Real)x);
-                erange.push_back(m.E_array[i]); erange.push_back(m.range_ep0[i]);
-                erange.push_back(m.range_ep1[i]); erange.push_back(0);
+                erange.push_back((Real)m.E_array[i]); erange.push_back((Real)m.range_ep0[i]);
+                erange.push_back((Real)m.range_ep1[i]); erange.push_back(0);
             }
             eoff += m.meke;
             for (int i = 0; i < m.mge; ++i) {
@@ -1058,7 +1082,7 @@ struct Engine : EngineBase {
             return cudaMemcpy(d.p, src, bytes, cudaMemcpyHostToDevice);
         };
         CK(up(d_etab, etab.data(), etab.size() * sizeof(Real)));
-        CK(up(d_erange, erange.data(), erange.size() * sizeof(RT)));
+        CK(up(d_erange, erange.data(), erange.size() * sizeof(Real)));
         CK(up(d_gtab, gtab.data(), gtab.size() * sizeof(Real)));
         CK(up(d_pmax, pmax.data(), pmax.size() * sizeof(Real)));
         CK(up(d_ray, ray.data(), ray.size() * sizeof(Real)));
@@ -1070,7 +1094,7 @@ struct Engine : EngineBase {
         CK(up(d_msi, msi.data(), msi.size() * sizeof(int)));
         if (sizeof(Real) == 4) CK(cudaMemcpyToSymbol(c_med_f, meds.data(), nmed * sizeof(MedScalars<Real>)));
         else CK(cudaMemcpyToSymbol(c_med_d, meds.data(), nmed * sizeof(MedScalars<Real>)));
-        T.etab = (const Real *)d_etab.p; T.erange = (const RT *)d_erange.p; T.gtab = (const Real *)d_gtab.p;
+        T.etab = (const Real *)d_etab.p; T.erange = (const Real *)d_erange.p; T.gtab = (const Real *)d_gtab.p;
         T.pmax = (const Real *)d_pmax.p; T.ray = (const Real *)d_ray.p; T.ray_i = (const int *)d_rayi.p;
         T.shell = (const Real *)d_shell.p; T.shell_at = (const int *)d_shellat.p; T.elem = (const Real *)d_elem.p;
         T.ms = (const Real *)d_ms.p; T.ms_i = (const int *)d_msi.p;
@@ -1145,13 +1169,20 @@ struct Engine : EngineBase {
     int run(const Source &S, long long first, long long n, int nbatch, uint32_t seed, cudaStream_t st,
             std::string &err) override {
         if (!G.xb) { err = "geometry not set"; return EGSGPU_ERR_STATE; }
-        unsigned cap = cfg.capacity > 0 ? (unsigned)std::min<long long>(cfg.capacity, 0x7fffffffLL) : (1u << 24);
+        unsigned cap = cfg.capacity > 0 ? (unsigned)std::min<long long>(cfg.capacity, 0x7fffffffLL) : (1u << 25);
         if (int rc = ensure_queues(cap, err)) return rc;
+        // Chunk autotuner: histories per wavefront are grown while the fullest
+        // queue stays below a third of its capacity and shrunk above two
+        // thirds; results do not depend on the chunking.
         long long chunk = cfg.chunk;
-        if (chunk <= 0) {
-            double emax = S.spectrum == 0 ? S.energy : 20.0;
-            double per = (S.charge == 0 ? 12.0 : 16.0) + 8.0 * emax;
-            chunk = std::max<long long>(1024, (long long)(capacity / per));
+        const bool tune = chunk <= 0;
+        if (tune) {
+            if (tuned_chunk <= 0) {
+                double emax = std::max(S.energy, 0.1);
+                double per = (S.charge == 0 ? 12.0 : 16.0) + 8.0 * emax;
+                tuned_chunk = std::max<long long>(1024, (long long)(capacity / per));
+            }
+            chunk = tuned_chunk;
         }
         const int bs = cfg.block_size > 0 ? cfg.block_size : 128;
         const int cps = cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm : 8;
@@ -1167,20 +1198,31 @@ struct Engine : EngineBase {
         P.seed = seed;
         unsigned *counts = (unsigned *)d_counts.p;
         long long per_batch = n / nbatch;
+        if (!events_ready) {
+            for (auto &e : ev) CK(cudaEventCreate(&e));
+            events_ready = true;
+        }
+        bool e_pending = false;
         for (int b = 0; b < nbatch; ++b) {
             long long b0 = first + b * per_batch, bn = (b == nbatch - 1) ? n - b * per_batch : per_batch;
             for (long long c0 = b0; c0 < b0 + bn; c0 += chunk) {
                 long long cn = std::min(chunk, b0 + bn - c0);
                 int cur = 0;
+                unsigned peak = 0;
                 CK(cudaMemsetAsync(counts, 0, 8 * sizeof(unsigned), st));
                 P.pout = q[0]; P.eout = q[2];
+                CK(cudaEventRecord(ev[0], st));
                 k_source<Real><<<(unsigned)((cn + 255) / 256), 256, 0, st>>>(P, S, c0, cn);
                 CK(cudaGetLastError());
+                CK(cudaEventRecord(ev[1], st));
+                bool src_pending = true;
                 for (int round = 0; round < 100000; ++round) {
                     unsigned h[8];
                     CK(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, st));
                     CK(cudaStreamSynchronize(st));
+                    if (src_pending) { prof_take(0, 0); src_pending = false; }
                     unsigned np = h[2 * cur], ne = h[4 + 2 * cur];
+                    peak = std::max(peak, std::max(np, ne));
                     if (np > capacity || ne > capacity) {
                         err = "particle queue capacity exceeded; lower egsgpu_config.chunk or raise capacity";
                         return EGSGPU_ERR_CAPACITY;
@@ -1193,12 +1235,17 @@ struct Engine : EngineBase {
                     if (np) {
                         P.pin = q[cur]; P.ein = q[2 + cur];
                         int g = (int)std::min<long long>(grid, (np + bs - 1) / bs);
+                        CK(cudaEventRecord(ev[2], st));
                         k_photon<Real><<<g, bs, 0, st>>>(P);
                         CK(cudaGetLastError());
+                        CK(cudaEventRecord(ev[3], st));
                     }
                     CK(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, st));
                     CK(cudaStreamSynchronize(st));
+                    if (np) prof_take(1, 1);
+                    if (e_pending) { prof_take(2, 2); e_pending = false; }
                     ne = h[4 + 2 * cur];
+                    peak = std::max(peak, ne);
                     if (ne > capacity) {
                         err = "particle queue capacity exceeded; lower egsgpu_config.chunk or raise capacity";
                         return EGSGPU_ERR_CAPACITY;
@@ -1206,15 +1253,27 @@ struct Engine : EngineBase {
                     if (ne) {
                         P.ein = q[2 + cur]; P.pout = q[nxt]; P.eout = q[2 + nxt];
                         int g = (int)std::min<long long>(grid, (ne + bs - 1) / bs);
+                        CK(cudaEventRecord(ev[4], st));
                         k_electron<Real><<<g, bs, 0, st>>>(P);
                         CK(cudaGetLastError());
+                        CK(cudaEventRecord(ev[5], st));
+                        e_pending = true;
                     }
                     cur = nxt;
                 }
+                if (e_pending) { CK(cudaStreamSynchronize(st)); prof_take(2, 2); e_pending = false; }
+                if (tune && cn == chunk) {
+                    if (peak < capacity / 3 && chunk < (1LL << 30)) tuned_chunk = chunk = chunk * 2;
+                    else if (peak > 2 * (capacity / 3)) tuned_chunk = chunk = std::max<long long>(1024, chunk / 2);
+                }
             }
+            CK(cudaEventRecord(ev[6], st));
             k_batch<<<std::max(1, std::min(4 * sm_count, (int)((nvox + 255) / 256))), 256, 0, st>>>(
                 (double *)d_dose.p, (double *)d_sum.p, (double *)d_sum2.p, nvox);
             CK(cudaGetLastError());
+            CK(cudaEventRecord(ev[7], st));
+            CK(cudaStreamSynchronize(st));
+            prof_take(3, 3);
         }
         CK(cudaStreamSynchronize(st));
         int e[2];
@@ -1258,7 +1317,7 @@ static int get_tallies_impl(egsgpu_handle *h, E *eng, double *sum, double *sum2,
         CK(cudaMemcpy(c, eng->d_counters.p, sizeof(c), cudaMemcpyDeviceToHost));
         totals[0] = (double)h->nhist; totals[1] = h->nbatch; totals[2] = en[0]; totals[3] = en[1];
         totals[4] = (double)(c[CNT_PSTEP] + c[CNT_ESTEP]); totals[5] = (double)c[CNT_PSTEP];
-        totals[6] = (double)c[CNT_ESTEP]; totals[7] = (double)c[CNT_PUSH];
+        totals[6] = (double)c[CNT_ESTEP]; totals[7] = (double)(c[CNT_PUSH] + c[CNT_EPUSH]);
     }
     return 0;
 }
@@ -1416,12 +1475,28 @@ int egsgpu_reset(egsgpu_handle *h) {
         CK(cudaMemset(eng->d_energy.p, 0, 2 * sizeof(double)));
         CK(cudaMemset(eng->d_counters.p, 0, CNT_N * sizeof(unsigned long long)));
         CK(cudaMemset(eng->d_error.p, 0, 2 * sizeof(int)));
+        for (int k = 0; k < 4; ++k) { eng->prof_ms[k] = 0; eng->prof_n[k] = 0; }
         return 0;
     };
     int rc = h->cfg.precision == 32 ? reset((Engine<float> *)h->eng.get()) : reset((Engine<double> *)h->eng.get());
     if (rc) return rc;
     h->nhist = 0; h->nbatch = 0;
     return 0;
+}
+
+int egsgpu_get_profile(egsgpu_handle *h, double *out) {
+    if (!h || !out || !h->have_geom) return EGSGPU_ERR_ARG;
+    std::string &err = h->err;
+    auto get = [&](auto *eng) -> int {
+        unsigned long long c[CNT_N];
+        CK(cudaMemcpy(c, eng->d_counters.p, sizeof(c), cudaMemcpyDeviceToHost));
+        for (int k = 0; k < 4; ++k) { out[k] = eng->prof_ms[k]; out[4 + k] = (double)eng->prof_n[k]; }
+        out[8] = (double)c[CNT_PSTEP]; out[9] = (double)c[CNT_ESTEP];
+        out[10] = (double)c[CNT_PUSH]; out[11] = (double)c[CNT_EPUSH];
+        out[12] = (double)c[CNT_INTER]; out[13] = (double)c[CNT_EINTER];
+        return 0;
+    };
+    return h->cfg.precision == 32 ? get((Engine<float> *)h->eng.get()) : get((Engine<double> *)h->eng.get());
 }
 
 int egsgpu_get_tallies(egsgpu_handle *h, double *sum, double *sum2, double *totals) {

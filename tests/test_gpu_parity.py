@@ -6,9 +6,11 @@ Three levels, following the reference's lack of transport golden values:
     deposited energies agree to rounding except where a last-ulp difference in
     a transcendental flips a rejection test;
   * statistically: FP32 and FP64 voxel doses against the oracle inside the
-    combined 2-sigma band (expected coverage 95.4%; we require >= 93% of the
-    voxels above 20% of Dmax, >= 99% within 3 sigma, and the total deposited
-    energy within 3 sigma);
+    combined 2-sigma band of 40-batch estimates (noise alone gives 94.8%
+    within 2 sigma and 99.5% within 3 sigma for t with 39 degrees of freedom;
+    we require >= 90% and >= 98% of the voxels above 10% of Dmax, a mean
+    squared deviation below 1.35 sigma^2, and the total deposited energy
+    within 3 sigma);
   * exactly: energy conservation per run, and independence of the results
     from the chunking of histories into wavefronts.
 """
@@ -85,11 +87,12 @@ def test_history_by_history_fp64(name, wl):
 @pytest.mark.parametrize("name", ["water_photon_2MeV", "water_electron_20MeV", "slab_spectrum"])
 def test_statistical_dose_band(name, precision):
     wl = dict(CASES)[name]
-    n_gpu = {"water_photon_2MeV": 400000, "water_electron_20MeV": 40000, "slab_spectrum": 400000}[name]
+    n_gpu = {"water_photon_2MeV": 800000, "water_electron_20MeV": 80000, "slab_spectrum": 800000}[name]
     n_ora = n_gpu // 4
     eng, ora = make_pair(wl, precision=precision)
-    eng.run(n_gpu, nbatch=10, seed=11)
-    ora.run(n_ora, nbatch=10, seed=12, threads=8)
+    nb = 40
+    eng.run(n_gpu, nbatch=nb, seed=11)
+    ora.run(n_ora, nbatch=nb, seed=12, threads=8)
     sg, s2g, tg = eng.tallies()
     so, s2o, to = ora.tallies()
 
@@ -98,14 +101,17 @@ def test_statistical_dose_band(name, precision):
         var = np.maximum(s2 / nb - m * m, 0) / (nb - 1)
         return s / n, np.sqrt(var) * nb / n   # per-history mean and its sigma
 
-    dg, eg_ = mean_sigma(sg, s2g, 10, n_gpu)
-    do, eo = mean_sigma(so, s2o, 10, n_ora)
+    dg, eg_ = mean_sigma(sg, s2g, nb, n_gpu)
+    do, eo = mean_sigma(so, s2o, nb, n_ora)
     dmax = max(dg.max(), do.max())
-    sel = (do > 0.2 * dmax)
-    assert sel.sum() > 20
+    sel = (do > 0.1 * dmax)
+    assert sel.sum() > 50
     z = np.abs(dg[sel] - do[sel]) / np.sqrt(eg_[sel] ** 2 + eo[sel] ** 2 + 1e-300)
-    frac2, frac3 = np.mean(z < 2), np.mean(z < 3)
-    assert frac2 >= 0.93 and frac3 >= 0.99, (name, precision, frac2, frac3)
+    # 40-batch sigma estimates: |t_39| < 2 for 94.8% and < 3 for 99.5% of noise-only
+    # voxels, and E[t^2] = 39/37; neighbouring voxels are correlated through
+    # shared histories, so the band fractions get some slack.
+    frac2, frac3, chi2 = np.mean(z < 2), np.mean(z < 3), np.mean(z * z)
+    assert frac2 >= 0.90 and frac3 >= 0.98 and chi2 < 1.35, (name, precision, frac2, frac3, chi2)
     # total deposited energy per history
     Eg, Eo = tg[2] / n_gpu, to[2] / n_ora
     # batch estimate of the sigma of the total
@@ -141,8 +147,9 @@ def test_chunking_invariance(precision):
         eng.set_history_tally(0, n)
         eng.run(n, nbatch=1, seed=3)
         res.append(eng.history_tally())
-    # same streams, same arithmetic: identical per-history results
-    assert np.array_equal(res[0], res[1])
+    # same streams, same arithmetic: identical per-history results up to the
+    # order of the FP64 atomic additions of one history's deposits
+    assert np.allclose(res[0], res[1], rtol=1e-12, atol=1e-12)
 
 
 def test_checkpoint_restore_roundtrip():

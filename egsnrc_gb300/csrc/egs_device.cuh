@@ -73,6 +73,10 @@ struct Source {
 
 // -------------------------------------------------------------- queues ----
 // Structure-of-arrays particle queue in HBM.  Photon queues ignore iq.
+// A particle parked mid-flight (a warp gave it up when its lanes ran low)
+// carries its transport state: st = 0 fresh; photons st = 1 with aux[0] the
+// remaining mean free paths; electrons st = 1 (new step sequence) or
+// st = 2 | 4*compute_tstep with aux = {demfp, total_de, total_tstep, sig0}.
 template <class Real>
 struct Queue {
     Real *x, *y, *z, *u, *v, *w, *E, *wt;
@@ -80,6 +84,8 @@ struct Queue {
     int8_t *iq;
     uint32_t *hist, *n;
     unsigned long long *sid;
+    uint8_t *st;
+    Real *aux0, *aux1, *aux2, *aux3;
     unsigned int *count;  // device counter (pushes)
     unsigned int capacity;
 };

@@ -394,11 +394,12 @@ __device__ inline void pair(const MedScalars<Real> &M, Particle<Real> &p, Real &
 }
 
 // ------------------------------------------------------ multiple scatter ----
-struct MsState { bool find_index; int i, j; double omega2; };
+template <class Real>
+struct MsState { bool find_index; int i, j; Real omega2; };
 
 // mscat, spin effects off (src/egsnrc.mortran:2984-3136)
 template <class Real>
-__device__ inline void mscat(const Tables<Real> &T, Rng &r, Real lambda, Real chia2, Real q1, MsState &st,
+__device__ inline void mscat(const Tables<Real> &T, Rng &r, Real lambda, Real chia2, Real q1, MsState<Real> &st,
                              Real &cost, Real &sint, int &err) {
     if (lambda <= (Real)13.8) {
         Real sprob = urand<Real>(r), explambda = dexp(-lambda);
@@ -475,7 +476,7 @@ __device__ inline void mscat(const Tables<Real> &T, Rng &r, Real lambda, Real ch
             Real x1 = (Real)0.5 * (1 - xi) * a;
             u = u + xi * du * (1 + x1 * (1 - xi * a));
         } else u = u - du / a * (1 - dsqrt(1 + xi * a * (2 + a)));
-        Real om = (Real)st.omega2;
+        Real om = st.omega2;
         xi = om * u / (1 + (Real)0.5 * om - u);
         if (xi > (Real)1.99999) xi = (Real)1.99999;
         cost = 1 - xi;
@@ -506,7 +507,7 @@ __device__ inline void msdist_pII(const Tables<Real> &T, const MedScalars<Real> 
     Real q1 = 2 * chia2 * (chilog * (1 + chia2) - 1);
     Real gamma = 6 * chia2 * (1 + chia2) * (chilog * (1 + 2 * chia2) - 2) / q1;
     Real xi = q1 * lambda;
-    MsState st;
+    MsState<Real> st;
     st.find_index = true; st.i = 0; st.j = 0; st.omega2 = 0;
     Real w1, sint1, w2, sint2;
     mscat(T, p.rng, lambda, chia2, xi, st, w1, sint1, err);

@@ -62,7 +62,13 @@ struct Params {
     unsigned long long *counters;         // CNT_*
     int *error;                           // [0] capacity, [1] loop cap
     uint32_t seed;
+    int requeue_lanes;                    // park survivors of warps this sparse (0 = never)
 };
+
+// A warp whose queue is exhausted parks its particles in the next queue once
+// this few of its lanes are still busy (only when the launch is large enough
+// for the next round to refill warps).
+constexpr unsigned REQUEUE_MIN = 32768;
 
 // ------------------------------------------------------------- tallies ----
 template <class Real>
@@ -103,6 +109,7 @@ __device__ inline void q_store(const Queue<Real> &q, unsigned i, const Particle<
     q.E[i] = p.E; q.wt[i] = p.wt; q.ir[i] = p.ir;
     if (q.iq) q.iq[i] = (int8_t)p.iq;
     q.hist[i] = p.rng.hist; q.n[i] = p.rng.n; q.sid[i] = p.rng.sid;
+    q.st[i] = 0;
 }
 template <class Real>
 __device__ inline void q_load(const Queue<Real> &q, unsigned i, uint32_t seed, Particle<Real> &p) {
@@ -113,21 +120,61 @@ __device__ inline void q_load(const Queue<Real> &q, unsigned i, uint32_t seed, P
     p.rng.init(seed, q.hist[i], q.sid[i], q.n[i]);
 }
 // Warp-aggregated append: the lanes that reach the push together share one
-// atomic on the queue counter.
+// atomic on the queue counter.  Returns the slot, or ~0u when the queue is full.
 template <class Real>
-__device__ inline void q_push(const Params<Real> &P, const Queue<Real> &q, const Particle<Real> &p,
-                              unsigned long long &npush) {
+__device__ inline unsigned q_slot(const Params<Real> &P, const Queue<Real> &q) {
     cg::coalesced_group g = cg::coalesced_threads();
     unsigned base = 0;
     if (g.thread_rank() == 0) base = atomicAdd(q.count, (unsigned)g.size());
     base = g.shfl(base, 0);
     unsigned i = base + g.thread_rank();
-    if (i < q.capacity) {
+    if (i < q.capacity) return i;
+    atomicExch(P.error + 0, 1);
+    return ~0u;
+}
+template <class Real>
+__device__ inline void q_push(const Params<Real> &P, const Queue<Real> &q, const Particle<Real> &p,
+                              unsigned long long &npush) {
+    unsigned i = q_slot(P, q);
+    if (i != ~0u) {
         q_store(q, i, p);
         ++npush;
-    } else {
-        atomicExch(P.error + 0, 1);
     }
+}
+
+// ANNIH_AT_REST (src/egsnrc.mortran:186-223): two back-to-back photons of
+// rest energy, the first continuing the positron's stream.
+template <class Real>
+__device__ inline void annih_at_rest(const Params<Real> &P, const Queue<Real> &qp, Particle<Real> &p,
+                                     unsigned long long &npush, int &err) {
+    const Real rm = (Real)RM;
+    Real costhe = urand<Real>(p.rng);
+    costhe = 2 * costhe - 1;
+    Real sinthe = dsqrt(dmax((Real)0, (1 - costhe) * (1 + costhe)));
+    Azim<Real> az = azimuth<Real>(p.rng, err);
+    Particle<Real> g1 = p, g2 = p;
+    g1.E = rm; g1.iq = 0; g1.u = sinthe * az.c; g1.v = sinthe * az.s; g1.w = costhe;
+    g2.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
+    g2.E = rm; g2.iq = 0; g2.u = -g1.u; g2.v = -g1.v; g2.w = -g1.w;
+    q_push(P, qp, g1, npush);
+    q_push(P, qp, g2, npush);
+}
+
+// Queue a new electron/positron, or -- when it is already at or below the
+// cut-off -- do its :ECUT-DISCARD: right here (deposit, and annihilation at
+// rest for a positron, on its own stream): what ELECTR would do first.
+template <class Real>
+__device__ inline void push_charged(const Params<Real> &P, const Queue<Real> &qe, const Queue<Real> &qp,
+                                    Particle<Real> &q, Acc<Real> &acc, unsigned long long &npush,
+                                    double &edep_tot, int &err) {
+    if (q.E <= P.T.ecut) {
+        Real edep = q.E - (Real)RM;
+        deposit(P, acc, q.ir, q.rng.hist, edep * q.wt);
+        edep_tot += (double)(edep * q.wt);
+        if (q.iq > 0) annih_at_rest(P, qp, q, npush, err);
+        return;
+    }
+    q_push(P, qe, q, npush);
 }
 
 // ----------------------------------------------------------- geometry ----
@@ -273,7 +320,21 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
     double edep_tot = 0, esc_tot = 0;
     int err = 0;
     const Real rm = (Real)RM;
+    const bool requeue = P.requeue_lanes > 0 && nq >= REQUEUE_MIN;
     while (true) {
+        if (exhausted && requeue) {
+            unsigned busy = __ballot_sync(0xffffffffu, alive);
+            if (__popc(busy) <= P.requeue_lanes) {   // park the survivors and retire the warp
+                if (alive) {
+                    unsigned i = q_slot(P, P.pout);
+                    if (i != ~0u) {
+                        q_store(P.pout, i, p);
+                        if (s.state != 0) { P.pout.st[i] = 1; P.pout.aux0[i] = s.dpmfp; }
+                    }
+                }
+                break;
+            }
+        }
         unsigned need = __ballot_sync(0xffffffffu, !alive);
         if (need && !exhausted) {
             unsigned base = 0;
@@ -287,6 +348,13 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
                     alive = true;
                     s.state = 0;
                     s.nsteps = 0;
+                    if (P.pin.st[idx]) {   // resume a parked photon
+                        s.state = 1;
+                        s.medium = G.med[p.ir];
+                        s.rhor = G.rhor[p.ir];
+                        s.gle = dlog(p.E);
+                        s.dpmfp = P.pin.aux0[idx];
+                    }
                 }
             }
         }
@@ -355,8 +423,8 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
             Particle<Real> q = p;
             q.E = E2; q.iq = iq2; q.u = u2; q.v = v2; q.w = w2;
             q.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
-            q_push(P, P.ein, p, npush);
-            q_push(P, P.ein, q, npush);
+            push_charged(P, P.ein, P.pout, p, acc, npush, edep_tot, err);
+            push_charged(P, P.ein, P.pout, q, acc, npush, edep_tot, err);
             alive = false;
             continue;
         }
@@ -367,13 +435,13 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
             e.iq = -1;
             e.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
             if (edep > 0) { deposit(P, acc, p.ir, p.rng.hist, edep * p.wt); edep_tot += (double)(edep * p.wt); }
-            q_push(P, P.ein, e, npush);
+            push_charged(P, P.ein, P.pout, e, acc, npush, edep_tot, err);
             s.state = 0;
             continue;
         }
         Real edep = photo(T, M, p, s.gle, err);
         if (edep > 0) { deposit(P, acc, p.ir, p.rng.hist, edep * p.wt); edep_tot += (double)(edep * p.wt); }
-        q_push(P, P.ein, p, npush);
+        push_charged(P, P.ein, P.pout, p, acc, npush, edep_tot, err);
         alive = false;
     }
     acc_flush(P, acc);
@@ -429,7 +497,7 @@ __device__ inline Real drange(const Tables<Real> &T, const MedScalars<Real> &M, 
                             Real el1, Real el2) {
     const Real *r = erow(T, M, lel);
     Real fedep = 1 - e2 / e1;
-    Real elktmp = 0.5 * (el1 + el2 + 0.25 * fedep * fedep * (1 + fedep * (1 + 0.875 * fedep)));
+    Real elktmp = (Real)0.5 * (el1 + el2 + (Real)0.25 * fedep * fedep * (1 + fedep * (1 + (Real)0.875 * fedep)));
     Real d0 = qel ? (Real)r[6] : (Real)r[4], d1 = qel ? (Real)r[7] : (Real)r[5];
     Real dedxmid = 1 / (d1 * elktmp + d0);
     Real aux = d1 * dedxmid;
@@ -446,7 +514,7 @@ __device__ inline Real eloss(const Tables<Real> &T, const MedScalars<Real> &M, i
     Real aux = d1 / dedxmid;
     Real de = dedxmid * step * rhof;
     Real fedep = de / eke;
-    return de * (1 - 0.5 * fedep * aux * (1 - 0.333333 * fedep * (aux - 1 - 0.25 * fedep * (2 - aux * (4 - aux)))));
+    return de * (1 - (Real)0.5 * fedep * aux * (1 - (Real)0.333333 * fedep * (aux - 1 - (Real)0.25 * fedep * (2 - aux * (4 - aux)))));
 }
 // $COMPUTE-ELOSS-G (:3315-3351)
 template <class Real>
@@ -456,7 +524,7 @@ __device__ inline Real eloss_g(const Tables<Real> &T, const MedScalars<Real> &M,
     if (tuss >= step) return eloss(T, M, qel, step, eke, elke, lel, rhof);
     int lt = lel;
     tuss = (range - step) * rhof;
-    if (tuss <= 0) return eke - (Real)M.te * 0.99;
+    if (tuss <= 0) return eke - M.te * (Real)0.99;
     while (lt > 1 && tuss < rrow(T, M, lt)[1 + qel]) --lt;
     if (lt > M.meke - 1) lt = M.meke - 1;
     Real elktmp = (lt + 1 - (Real)M.eke0) / (Real)M.eke1, eketmp = rrow(T, M, lt + 1)[0];
@@ -480,7 +548,26 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
     double edep_tot = 0, esc_tot = 0;
     int err = 0;
     const Real rm = (Real)RM;
+    const bool requeue = P.requeue_lanes > 0 && nq >= REQUEUE_MIN;
     while (true) {
+        if (exhausted && requeue) {
+            unsigned busy = __ballot_sync(0xffffffffu, alive);
+            if (__popc(busy) <= P.requeue_lanes) {   // park the survivors and retire the warp
+                if (alive) {
+                    unsigned i = q_slot(P, P.eout);
+                    if (i != ~0u) {
+                        q_store(P.eout, i, p);
+                        if (s.state == 1) P.eout.st[i] = 1;
+                        else if (s.state == 2) {
+                            P.eout.st[i] = (uint8_t)(2 | (s.compute_tstep ? 4 : 0));
+                            P.eout.aux0[i] = s.demfp; P.eout.aux1[i] = s.total_de;
+                            P.eout.aux2[i] = s.total_tstep; P.eout.aux3[i] = s.sig0;
+                        }
+                    }
+                }
+                break;
+            }
+        }
         unsigned need = __ballot_sync(0xffffffffu, !alive);
         if (need && !exhausted) {
             unsigned base = 0;
@@ -498,6 +585,18 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                     s.nsteps = 0;
                     s.medium = G.med[p.ir];
                     s.rhor = G.rhor[p.ir];
+                    uint8_t st = P.ein.st[idx];
+                    if (st == 1) s.state = 1;
+                    else if (st & 2) {   // resume a parked condensed-history sequence
+                        const MedScalars<Real> &M = cmed<Real>(s.medium);
+                        s.state = 2;
+                        s.compute_tstep = (st & 4) ? 1 : 0;
+                        s.demfp = P.ein.aux0[idx]; s.total_de = P.ein.aux1[idx];
+                        s.total_tstep = P.ein.aux2[idx]; s.sig0 = P.ein.aux3[idx];
+                        s.eke = p.E - (Real)RM;
+                        s.elke = dlog(s.eke);
+                        s.lelke = min(max((int)(M.eke1 * s.elke + M.eke0), 1), M.meke);
+                    }
                 }
             }
         }
@@ -530,12 +629,12 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
             Real rhof = s.rhor, sig = s.sig0;
             Real tstep;
             const Real *rr = rrow(T, M, s.lelke);
-            if (sig <= 0) { tstep = 1e8; s.sig0 = (Real)1e-15; }
+            if (sig <= 0) { tstep = (Real)1e8; s.sig0 = (Real)1e-15; }
             else {
                 if (s.compute_tstep) {
                     s.total_de = (Real)s.demfp / (Real)sig;
                     Real eke = s.eke, elke = s.elke, ekef = eke - s.total_de;
-                    if (ekef <= M.E_array0) tstep = 1e8;
+                    if (ekef <= M.E_array0) tstep = (Real)1e8;
                     else {
                         Real elkef = dlog(ekef);
                         int lelkef = min(max((int)((Real)M.eke1 * elkef + (Real)M.eke0), 1), s.lelke);
@@ -669,7 +768,7 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                         s.demfp = s.demfp - (Real)(de * (Real)sig);
                         s.total_de = s.total_de - de;
                         s.total_tstep = s.total_tstep - (Real)tvstep * (Real)rhof;
-                        if (s.total_tstep < 1e-9) s.demfp = 0;
+                        if (s.total_tstep < (Real)1e-9) s.demfp = 0;
                         if (!(s.demfp < (Real)1e-8)) continue;
                         // fictitious-cross-section rejection
                         const MedScalars<Real> &M2 = cmed<Real>(s.medium);
@@ -719,7 +818,7 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                                 costhe = dsqrt(dmin((Real)1, dcosth));
                                 rotate(a, b, c, sinthe, costhe, az, d.u, d.v, d.w);
                                 d.E = pese2; d.iq = -1;
-                                q_push(P, P.eout, d, npush);
+                                push_charged(P, P.eout, P.pout, d, acc, npush, edep_tot, err);
                                 s.state = 0;
                                 continue;
                             }
@@ -760,7 +859,7 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                                     costhe = dsqrt(dmin((Real)1, dcosth));
                                     rotate(a, b, c, sinthe, costhe, az, d.u, d.v, d.w);
                                     d.E = pese2; d.iq = iq_new;
-                                    q_push(P, P.eout, d, npush);
+                                    push_charged(P, P.eout, P.pout, d, acc, npush, edep_tot, err);
                                     s.state = 0;
                                     continue;
                                 }
@@ -874,18 +973,7 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
             Real edep = p.E - rm;
             deposit(P, acc, p.ir, p.rng.hist, edep * p.wt);
             edep_tot += (double)(edep * p.wt);
-            if (p.iq > 0) {   // ANNIH_AT_REST (src/egsnrc.mortran:186-223)
-                Real costhe = urand<Real>(p.rng);
-                costhe = 2 * costhe - 1;
-                Real sinthe = dsqrt(dmax((Real)0, (1 - costhe) * (1 + costhe)));
-                Azim<Real> az = azimuth<Real>(p.rng, err);
-                Particle<Real> g1 = p, g2 = p;
-                g1.E = rm; g1.iq = 0; g1.u = sinthe * az.c; g1.v = sinthe * az.s; g1.w = costhe;
-                g2.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
-                g2.E = rm; g2.iq = 0; g2.u = -g1.u; g2.v = -g1.v; g2.w = -g1.w;
-                q_push(P, P.pout, g1, npush);
-                q_push(P, P.pout, g2, npush);
-            }
+            if (p.iq > 0) annih_at_rest(P, P.pout, p, npush, err);
             alive = false;
         }
     }
@@ -1144,7 +1232,8 @@ struct Engine : EngineBase {
 
     int ensure_queues(unsigned cap, std::string &err) {
         if (cap <= capacity) return 0;
-        size_t per = 8 * sizeof(Real) + sizeof(int) + sizeof(int8_t) + 2 * sizeof(uint32_t) + sizeof(unsigned long long);
+        size_t per = 12 * sizeof(Real) + sizeof(int) + 2 * sizeof(int8_t) + 2 * sizeof(uint32_t) +
+                     sizeof(unsigned long long);
         CK(d_counts.alloc(8 * sizeof(unsigned)));
         for (int k = 0; k < 4; ++k) {
             CK(qmem[k].alloc((size_t)cap * per + 1024));
@@ -1159,6 +1248,11 @@ struct Engine : EngineBase {
             Q.iq = (k >= 2) ? (int8_t *)take(cap) : nullptr;
             Q.hist = (uint32_t *)take(cap * sizeof(uint32_t)); Q.n = (uint32_t *)take(cap * sizeof(uint32_t));
             Q.sid = (unsigned long long *)take(cap * sizeof(unsigned long long));
+            Q.st = (uint8_t *)take(cap);
+            Q.aux0 = (Real *)take(cap * sizeof(Real));
+            Q.aux1 = (k >= 2) ? (Real *)take(cap * sizeof(Real)) : nullptr;
+            Q.aux2 = (k >= 2) ? (Real *)take(cap * sizeof(Real)) : nullptr;
+            Q.aux3 = (k >= 2) ? (Real *)take(cap * sizeof(Real)) : nullptr;
             Q.count = (unsigned *)d_counts.p + 2 * k;
             Q.capacity = cap;
         }
@@ -1196,6 +1290,7 @@ struct Engine : EngineBase {
         P.counters = (unsigned long long *)d_counters.p;
         P.error = (int *)d_error.p;
         P.seed = seed;
+        P.requeue_lanes = cfg.requeue_lanes == 0 ? 8 : (cfg.requeue_lanes < 0 ? 0 : cfg.requeue_lanes);
         unsigned *counts = (unsigned *)d_counts.p;
         long long per_batch = n / nbatch;
         if (!events_ready) {
@@ -1233,7 +1328,7 @@ struct Engine : EngineBase {
                     CK(cudaMemsetAsync(counts + 2 * nxt, 0, 2 * sizeof(unsigned), st));
                     CK(cudaMemsetAsync(counts + 4 + 2 * nxt, 0, 2 * sizeof(unsigned), st));
                     if (np) {
-                        P.pin = q[cur]; P.ein = q[2 + cur];
+                        P.pin = q[cur]; P.ein = q[2 + cur]; P.pout = q[nxt];
                         int g = (int)std::min<long long>(grid, (np + bs - 1) / bs);
                         CK(cudaEventRecord(ev[2], st));
                         k_photon<Real><<<g, bs, 0, st>>>(P);

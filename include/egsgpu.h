@@ -46,6 +46,9 @@ typedef struct {
     int ctas_per_sm;      /* resident CTAs per SM; 0 = default                       */
     long long chunk;      /* histories per wavefront chunk; 0 = automatic   */
     long long capacity;   /* particle-queue capacity per queue; 0 = automatic */
+    int requeue_lanes;    /* a warp whose queue is empty parks its particles for the
+                             next round once this few lanes are busy; 0 = default (8),
+                             -1 = never (results are identical either way) */
 } egsgpu_config;
 
 /* Source: egs++ EGS_ParallelBeam (sources/egs_parallel_beam) with a point

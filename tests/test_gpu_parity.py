@@ -198,7 +198,10 @@ def test_requeue_invariance(precision):
         eng.set_history_tally(0, n)
         eng.run(n, nbatch=1, seed=9)
         res.append(eng.history_tally())
-    assert np.allclose(res[0], res[1], rtol=1e-12, atol=1e-12)
+    # FP32: a parked particle's pending per-voxel FP32 partial sum is split in
+    # two, which regroups float additions (relative 1e-7 per deposit)
+    tol = 1e-12 if precision == 64 else 2e-5
+    assert np.allclose(res[0], res[1], rtol=tol, atol=tol)
 
 
 def test_checkpoint_restore_roundtrip():

@@ -64,28 +64,64 @@ def dist_setup(args):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """SM clocks and clock-event (throttle) reasons sampled during the timed
+    region through NVML in-process (libnvidia-ml via ctypes; read-only
+    queries), falling back to nvidia-smi once per second."""
 
-    def __init__(self, index=0):
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, index=0, period=0.2):
         self.index = index
-        self.samples = []
+        self.period = period
+        self.samples = []     # (sm_mhz, max_mhz, reasons_bitmask, power_w)
         self._stop = threading.Event()
         self._t = None
+        self._nvml = None
+        try:
+            import ctypes
+            L = ctypes.CDLL("libnvidia-ml.so.1")
+            if L.nvmlInit_v2() == 0:
+                h = ctypes.c_void_p()
+                if L.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(index), ctypes.byref(h)) == 0:
+                    self._nvml = (ctypes, L, h)
+        except Exception:
+            self._nvml = None
 
-    def _run(self):
+    def _sample_nvml(self):
+        ctypes, L, h = self._nvml
+        clk, mx, pw = ctypes.c_uint(0), ctypes.c_uint(0), ctypes.c_uint(0)
+        rs = ctypes.c_ulonglong(0)
+        L.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk))          # NVML_CLOCK_SM
+        L.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx))
+        L.nvmlDeviceGetPowerUsage(h, ctypes.byref(pw))
+        L.nvmlDeviceGetCurrentClocksThrottleReasons(h, ctypes.byref(rs))
+        self.samples.append((float(clk.value), float(mx.value), int(rs.value), pw.value / 1e3))
+
+    def _sample_smi(self):
         q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
+        out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                              "--format=csv,noheader,nounits"], stdout=subprocess.PIPE,
+                             stderr=subprocess.DEVNULL, text=True, timeout=5).stdout.strip()
+        f = [x.strip() for x in out.split(",")]
+        bits = 0
+        for b, v in zip((0x8, 0x40, 0x20, 0x4), f[3:7]):
+            if v.lower() == "active":
+                bits |= b
+        self.samples.append((float(f[0]), float(f[1]), bits, float(f[2]) if f[2][:1].isdigit() else 0.0))
+
+    def _run(self):
         while not self._stop.is_set():
             try:
-                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
-                                      "--format=csv,noheader,nounits"], stdout=subprocess.PIPE,
-                                     stderr=subprocess.DEVNULL, text=True, timeout=5).stdout.strip()
-                if out:
-                    self.samples.append([x.strip() for x in out.split(",")])
+                if self._nvml:
+                    self._sample_nvml()
+                else:
+                    self._sample_smi()
             except Exception:
                 pass
-            self._stop.wait(0.2)
+            self._stop.wait(self.period if self._nvml else 1.0)
 
     def __enter__(self):
         self._t = threading.Thread(target=self._run, daemon=True)
@@ -99,13 +135,12 @@ class ClockSampler:
     def summary(self):
         if not self.samples:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 3 + i and
-                          s[3 + i].lower() == "active"})
-        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+        sm = [s[0] for s in self.samples]
+        reasons = sorted({name for s in self.samples for bit, name in self.REASONS.items() if s[2] & bit})
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(s[1] for s in self.samples),
+                "reasons": reasons, "samples": len(self.samples),
+                "power_w_max": max(s[3] for s in self.samples),
+                "source": "nvml" if self._nvml else "nvidia-smi"}
 
 
 def measured_peak_hbm():

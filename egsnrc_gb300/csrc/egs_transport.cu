@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -61,6 +62,7 @@ struct Params {
     double *energy;                       // [0] deposited, [1] escaped
     unsigned long long *counters;         // CNT_*
     int *error;                           // [0] capacity, [1] loop cap
+    unsigned *peak;                       // largest queue length seen (autotuner input)
     uint32_t seed;
     int requeue_lanes;                    // park survivors of warps this sparse (0 = never)
 };
@@ -310,6 +312,7 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
     const Geom<Real> &G = P.G;
     const unsigned lane = threadIdx.x & 31u;
     const unsigned nq = *P.pin.count < P.pin.capacity ? *P.pin.count : P.pin.capacity;
+    if (threadIdx.x == 0 && blockIdx.x == 0) atomicMax(P.peak, *P.pin.count);
     __shared__ unsigned s_dummy;
     (void)s_dummy;
     Particle<Real> p;
@@ -539,6 +542,7 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
     const Geom<Real> &G = P.G;
     const unsigned lane = threadIdx.x & 31u;
     const unsigned nq = *P.ein.count < P.ein.capacity ? *P.ein.count : P.ein.capacity;
+    if (threadIdx.x == 0 && blockIdx.x == 0) atomicMax(P.peak, *P.ein.count);
     Particle<Real> p;
     ElecState<Real> s;
     Real edep_part = 0;   // continuous-loss deposits of the current particle
@@ -1073,6 +1077,9 @@ struct Engine : EngineBase {
     cudaEvent_t ev[8] = {};
     bool events_ready = false;
     long long tuned_chunk = 0;   // histories per wavefront chosen by the autotuner
+    long long best_chunk = 0;
+    double best_rate = 0;
+    bool tune_done = false;
 
     explicit Engine(const egsgpu_config &c) : cfg(c) {
         int dev = 0;
@@ -1080,8 +1087,13 @@ struct Engine : EngineBase {
         cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev);
     }
     ~Engine() {
-        if (events_ready)
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (events_ready) {
             for (auto &e : ev) cudaEventDestroy(e);
+            for (auto &e : gev) cudaEventDestroy(e);
+            cudaEventDestroy(ev_in);
+            cudaStreamDestroy(ws);
+        }
     }
     // accumulate the elapsed time between events 2k and 2k+1 (after a sync)
     void prof_take(int k, int slot) {
@@ -1234,7 +1246,7 @@ struct Engine : EngineBase {
         if (cap <= capacity) return 0;
         size_t per = 12 * sizeof(Real) + sizeof(int) + 2 * sizeof(int8_t) + 2 * sizeof(uint32_t) +
                      sizeof(unsigned long long);
-        CK(d_counts.alloc(8 * sizeof(unsigned)));
+        CK(d_counts.alloc(16 * sizeof(unsigned)));
         for (int k = 0; k < 4; ++k) {
             CK(qmem[k].alloc((size_t)cap * per + 1024));
             char *b = (char *)qmem[k].p;
@@ -1260,14 +1272,65 @@ struct Engine : EngineBase {
         return 0;
     }
 
+    // One CUDA graph holds ROUNDS wavefront rounds (photon kernel, then
+    // electron kernel, on alternating queue pairs; a launch whose queue is
+    // empty retires at once).  The host replays it until both queues are
+    // empty, reading the queue counters once per replay, so host-side stalls
+    // do not idle the GPU between rounds.
+    static constexpr int ROUNDS = 4;
+    cudaStream_t ws = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    cudaEvent_t gev[4 * ROUNDS] = {};
+    cudaEvent_t ev_in = nullptr;
+
+    int build_graph(const Params<Real> &P0, int grid, int bs, std::string &err) {
+        if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+        unsigned *counts = (unsigned *)d_counts.p;
+        CK(cudaStreamBeginCapture(ws, cudaStreamCaptureModeThreadLocal));
+        for (int r = 0; r < ROUNDS; ++r) {
+            int cur = r & 1, nxt = 1 - cur;
+            Params<Real> P = P0;
+            P.pin = q[cur]; P.ein = q[2 + cur]; P.pout = q[nxt]; P.eout = q[2 + nxt];
+            cudaMemsetAsync(counts + 2 * nxt, 0, 2 * sizeof(unsigned), ws);
+            cudaMemsetAsync(counts + 4 + 2 * nxt, 0, 2 * sizeof(unsigned), ws);
+            cudaEventRecord(gev[4 * r], ws);
+            k_photon<Real><<<grid, bs, 0, ws>>>(P);
+            cudaEventRecord(gev[4 * r + 1], ws);
+            cudaEventRecord(gev[4 * r + 2], ws);
+            k_electron<Real><<<grid, bs, 0, ws>>>(P);
+            cudaEventRecord(gev[4 * r + 3], ws);
+        }
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(ws, &g);
+        if (e != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(e); return EGSGPU_ERR_CUDA; }
+        e = cudaGraphInstantiate(&gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) { err = std::string("graph instantiate: ") + cudaGetErrorString(e); return EGSGPU_ERR_CUDA; }
+        return 0;
+    }
+
+    float elapsed(cudaEvent_t a, cudaEvent_t b) {
+        float ms = 0;
+        return cudaEventElapsedTime(&ms, a, b) == cudaSuccess ? ms : 0.f;
+    }
+
     int run(const Source &S, long long first, long long n, int nbatch, uint32_t seed, cudaStream_t st,
             std::string &err) override {
         if (!G.xb) { err = "geometry not set"; return EGSGPU_ERR_STATE; }
         unsigned cap = cfg.capacity > 0 ? (unsigned)std::min<long long>(cfg.capacity, 0x7fffffffLL) : (1u << 25);
         if (int rc = ensure_queues(cap, err)) return rc;
-        // Chunk autotuner: histories per wavefront are grown while the fullest
-        // queue stays below a third of its capacity and shrunk above two
-        // thirds; results do not depend on the chunking.
+        if (!events_ready) {
+            for (auto &e : ev) CK(cudaEventCreate(&e));
+            for (auto &e : gev) CK(cudaEventCreate(&e));
+            CK(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming));
+            CK(cudaStreamCreateWithFlags(&ws, cudaStreamNonBlocking));
+            events_ready = true;
+        }
+        // Chunk autotuner: histories per wavefront double while the fullest
+        // queue of a chunk stays below a third of its capacity and a doubling
+        // does not cost more than 10% of the measured throughput; a queue above
+        // two thirds halves the chunk.  Results do not depend on the chunking
+        // (every history owns its random-number streams).
         long long chunk = cfg.chunk;
         const bool tune = chunk <= 0;
         if (tune) {
@@ -1289,88 +1352,72 @@ struct Engine : EngineBase {
         P.energy = (double *)d_energy.p;
         P.counters = (unsigned long long *)d_counters.p;
         P.error = (int *)d_error.p;
+        P.peak = (unsigned *)d_counts.p + 8;
         P.seed = seed;
-        P.requeue_lanes = cfg.requeue_lanes == 0 ? 8 : (cfg.requeue_lanes < 0 ? 0 : cfg.requeue_lanes);
+        P.requeue_lanes = cfg.requeue_lanes > 0 ? cfg.requeue_lanes : 0;
+        P.pin = q[0]; P.ein = q[2]; P.pout = q[0]; P.eout = q[2];
+        if (int rc = build_graph(P, grid, bs, err)) return rc;
         unsigned *counts = (unsigned *)d_counts.p;
+        CK(cudaEventRecord(ev_in, st));
+        CK(cudaStreamWaitEvent(ws, ev_in, 0));
         long long per_batch = n / nbatch;
-        if (!events_ready) {
-            for (auto &e : ev) CK(cudaEventCreate(&e));
-            events_ready = true;
-        }
-        bool e_pending = false;
         for (int b = 0; b < nbatch; ++b) {
             long long b0 = first + b * per_batch, bn = (b == nbatch - 1) ? n - b * per_batch : per_batch;
             for (long long c0 = b0; c0 < b0 + bn; c0 += chunk) {
                 long long cn = std::min(chunk, b0 + bn - c0);
-                int cur = 0;
-                unsigned peak = 0;
-                CK(cudaMemsetAsync(counts, 0, 8 * sizeof(unsigned), st));
-                P.pout = q[0]; P.eout = q[2];
-                CK(cudaEventRecord(ev[0], st));
-                k_source<Real><<<(unsigned)((cn + 255) / 256), 256, 0, st>>>(P, S, c0, cn);
+                auto t_chunk = std::chrono::steady_clock::now();
+                CK(cudaMemsetAsync(counts, 0, 9 * sizeof(unsigned), ws));
+                CK(cudaEventRecord(ev[0], ws));
+                k_source<Real><<<(unsigned)((cn + 255) / 256), 256, 0, ws>>>(P, S, c0, cn);
                 CK(cudaGetLastError());
-                CK(cudaEventRecord(ev[1], st));
-                bool src_pending = true;
-                for (int round = 0; round < 100000; ++round) {
-                    unsigned h[8];
-                    CK(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, st));
-                    CK(cudaStreamSynchronize(st));
-                    if (src_pending) { prof_take(0, 0); src_pending = false; }
-                    unsigned np = h[2 * cur], ne = h[4 + 2 * cur];
-                    peak = std::max(peak, std::max(np, ne));
-                    if (np > capacity || ne > capacity) {
+                CK(cudaEventRecord(ev[1], ws));
+                unsigned h[9] = {};
+                bool done = false;
+                for (int rep = 0; rep < 100000 / ROUNDS && !done; ++rep) {
+                    CK(cudaGraphLaunch(gexec, ws));
+                    CK(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, ws));
+                    CK(cudaStreamSynchronize(ws));
+                    if (rep == 0) { prof_ms[0] += elapsed(ev[0], ev[1]); ++prof_n[0]; }
+                    for (int r = 0; r < ROUNDS; ++r) {
+                        prof_ms[1] += elapsed(gev[4 * r], gev[4 * r + 1]); ++prof_n[1];
+                        prof_ms[2] += elapsed(gev[4 * r + 2], gev[4 * r + 3]); ++prof_n[2];
+                    }
+                    if (h[8] > capacity || h[0] > capacity || h[4] > capacity) {
                         err = "particle queue capacity exceeded; lower egsgpu_config.chunk or raise capacity";
                         return EGSGPU_ERR_CAPACITY;
                     }
-                    if (np == 0 && ne == 0) break;
-                    int nxt = 1 - cur;
-                    // next queues start empty
-                    CK(cudaMemsetAsync(counts + 2 * nxt, 0, 2 * sizeof(unsigned), st));
-                    CK(cudaMemsetAsync(counts + 4 + 2 * nxt, 0, 2 * sizeof(unsigned), st));
-                    if (np) {
-                        P.pin = q[cur]; P.ein = q[2 + cur]; P.pout = q[nxt];
-                        int g = (int)std::min<long long>(grid, (np + bs - 1) / bs);
-                        CK(cudaEventRecord(ev[2], st));
-                        k_photon<Real><<<g, bs, 0, st>>>(P);
-                        CK(cudaGetLastError());
-                        CK(cudaEventRecord(ev[3], st));
-                    }
-                    CK(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, st));
-                    CK(cudaStreamSynchronize(st));
-                    if (np) prof_take(1, 1);
-                    if (e_pending) { prof_take(2, 2); e_pending = false; }
-                    ne = h[4 + 2 * cur];
-                    peak = std::max(peak, ne);
-                    if (ne > capacity) {
-                        err = "particle queue capacity exceeded; lower egsgpu_config.chunk or raise capacity";
-                        return EGSGPU_ERR_CAPACITY;
-                    }
-                    if (ne) {
-                        P.ein = q[2 + cur]; P.pout = q[nxt]; P.eout = q[2 + nxt];
-                        int g = (int)std::min<long long>(grid, (ne + bs - 1) / bs);
-                        CK(cudaEventRecord(ev[4], st));
-                        k_electron<Real><<<g, bs, 0, st>>>(P);
-                        CK(cudaGetLastError());
-                        CK(cudaEventRecord(ev[5], st));
-                        e_pending = true;
-                    }
-                    cur = nxt;
+                    done = (h[0] == 0 && h[4] == 0);
                 }
-                if (e_pending) { CK(cudaStreamSynchronize(st)); prof_take(2, 2); e_pending = false; }
+                if (!done) { err = "wavefront did not drain"; return EGSGPU_ERR_LOOP; }
                 if (tune && cn == chunk) {
-                    if (peak < capacity / 3 && chunk < (1LL << 30)) tuned_chunk = chunk = chunk * 2;
-                    else if (peak > 2 * (capacity / 3)) tuned_chunk = chunk = std::max<long long>(1024, chunk / 2);
+                    double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_chunk).count();
+                    double rate = cn / std::max(dt, 1e-9);
+                    unsigned peak = h[8];
+                    if (peak > 2 * (capacity / 3)) {
+                        tuned_chunk = chunk = std::max<long long>(1024, chunk / 2);
+                        tune_done = true;
+                    } else if (!tune_done) {
+                        if (best_rate > 0 && rate < 0.9 * best_rate) {
+                            tuned_chunk = chunk = best_chunk;
+                            tune_done = true;
+                        } else {
+                            if (rate > best_rate) { best_rate = rate; best_chunk = chunk; }
+                            if (peak < capacity / 3 && chunk < (1LL << 30)) tuned_chunk = chunk = chunk * 2;
+                            else tune_done = true;
+                        }
+                    }
                 }
             }
-            CK(cudaEventRecord(ev[6], st));
-            k_batch<<<std::max(1, std::min(4 * sm_count, (int)((nvox + 255) / 256))), 256, 0, st>>>(
+            CK(cudaEventRecord(ev[6], ws));
+            k_batch<<<std::max(1, std::min(4 * sm_count, (int)((nvox + 255) / 256))), 256, 0, ws>>>(
                 (double *)d_dose.p, (double *)d_sum.p, (double *)d_sum2.p, nvox);
             CK(cudaGetLastError());
-            CK(cudaEventRecord(ev[7], st));
-            CK(cudaStreamSynchronize(st));
-            prof_take(3, 3);
+            CK(cudaEventRecord(ev[7], ws));
+            CK(cudaStreamSynchronize(ws));
+            prof_ms[3] += elapsed(ev[6], ev[7]);
+            ++prof_n[3];
         }
-        CK(cudaStreamSynchronize(st));
+        CK(cudaStreamSynchronize(ws));
         int e[2];
         CK(cudaMemcpy(e, d_error.p, sizeof(e), cudaMemcpyDeviceToHost));
         if (e[0]) { err = "particle queue capacity exceeded"; return EGSGPU_ERR_CAPACITY; }
@@ -1589,6 +1636,7 @@ int egsgpu_get_profile(egsgpu_handle *h, double *out) {
         out[8] = (double)c[CNT_PSTEP]; out[9] = (double)c[CNT_ESTEP];
         out[10] = (double)c[CNT_PUSH]; out[11] = (double)c[CNT_EPUSH];
         out[12] = (double)c[CNT_INTER]; out[13] = (double)c[CNT_EINTER];
+        out[14] = (double)eng->tuned_chunk;
         return 0;
     };
     return h->cfg.precision == 32 ? get((Engine<float> *)h->eng.get()) : get((Engine<double> *)h->eng.get());

@@ -32,7 +32,7 @@ class Config(C.Structure):
     _fields_ = [("ecut", C.c_double), ("pcut", C.c_double), ("estepe", C.c_double), ("ximax", C.c_double),
                 ("skindepth", C.c_double), ("precision", C.c_int), ("block_size", C.c_int),
                 ("ctas_per_sm", C.c_int), ("chunk", C.c_longlong), ("capacity", C.c_longlong),
-                ("requeue_lanes", C.c_int)]
+                ("requeue_lanes", C.c_int), ("use_graph", C.c_int)]
 
 
 class SourceStruct(C.Structure):
@@ -205,13 +205,14 @@ class DoseEngine:
         return d, s
 
     def profile(self):
-        o = np.zeros(15)
+        o = np.zeros(16)
         self._check(self.L.egsgpu_get_profile(self.h, _dp(o)))
         keys = ("source", "photon", "electron", "batch")
         d = {"ms_" + k: o[i] for i, k in enumerate(keys)}
         d.update({"launches_" + k: int(o[4 + i]) for i, k in enumerate(keys)})
         d.update(photon_steps=o[8], electron_steps=o[9], photon_pushes=o[10], electron_pushes=o[11],
-                 photon_interactions=o[12], electron_interactions=o[13], chunk=int(o[14]))
+                 photon_interactions=o[12], electron_interactions=o[13], chunk=int(o[14]),
+                 graph=bool(o[15]))
         return d
 
     def set_history_tally(self, first, n):

@@ -1272,41 +1272,60 @@ struct Engine : EngineBase {
         return 0;
     }
 
-    // One CUDA graph holds ROUNDS wavefront rounds (photon kernel, then
-    // electron kernel, on alternating queue pairs; a launch whose queue is
-    // empty retires at once).  The host replays it until both queues are
-    // empty, reading the queue counters once per replay, so host-side stalls
-    // do not idle the GPU between rounds.
+    // ROUNDS wavefront rounds (photon kernel, then electron kernel, on
+    // alternating queue pairs; a launch whose queue is empty retires at once)
+    // are enqueued back to back and the host reads the queue counters once
+    // per ROUNDS, so host-side stalls do not idle the GPU between rounds.  The
+    // rounds are either launched directly, with CUDA events around every
+    // kernel, or replayed from a CUDA graph of the same launches.
     static constexpr int ROUNDS = 4;
     cudaStream_t ws = nullptr;
     cudaGraphExec_t gexec = nullptr;
     cudaEvent_t gev[4 * ROUNDS] = {};
     cudaEvent_t ev_in = nullptr;
+    bool graph_ok = true;
 
-    int build_graph(const Params<Real> &P0, int grid, int bs, std::string &err) {
-        if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+    cudaError_t enqueue_rounds(const Params<Real> &P0, int grid, int bs, bool events) {
         unsigned *counts = (unsigned *)d_counts.p;
-        CK(cudaStreamBeginCapture(ws, cudaStreamCaptureModeThreadLocal));
-        for (int r = 0; r < ROUNDS; ++r) {
+        cudaError_t e = cudaSuccess;
+        for (int r = 0; r < ROUNDS && e == cudaSuccess; ++r) {
             int cur = r & 1, nxt = 1 - cur;
             Params<Real> P = P0;
             P.pin = q[cur]; P.ein = q[2 + cur]; P.pout = q[nxt]; P.eout = q[2 + nxt];
-            cudaMemsetAsync(counts + 2 * nxt, 0, 2 * sizeof(unsigned), ws);
-            cudaMemsetAsync(counts + 4 + 2 * nxt, 0, 2 * sizeof(unsigned), ws);
-            cudaEventRecord(gev[4 * r], ws);
+            if ((e = cudaMemsetAsync(counts + 2 * nxt, 0, 2 * sizeof(unsigned), ws))) break;
+            if ((e = cudaMemsetAsync(counts + 4 + 2 * nxt, 0, 2 * sizeof(unsigned), ws))) break;
+            if (events && (e = cudaEventRecord(gev[4 * r], ws))) break;
             k_photon<Real><<<grid, bs, 0, ws>>>(P);
-            cudaEventRecord(gev[4 * r + 1], ws);
-            cudaEventRecord(gev[4 * r + 2], ws);
+            if ((e = cudaGetLastError())) break;
+            if (events && (e = cudaEventRecord(gev[4 * r + 1], ws))) break;
+            if (events && (e = cudaEventRecord(gev[4 * r + 2], ws))) break;
             k_electron<Real><<<grid, bs, 0, ws>>>(P);
-            cudaEventRecord(gev[4 * r + 3], ws);
+            if ((e = cudaGetLastError())) break;
+            if (events && (e = cudaEventRecord(gev[4 * r + 3], ws))) break;
         }
+        return e;
+    }
+
+    // Captures the rounds (without events) into a graph; on any failure the
+    // engine keeps launching directly.
+    void build_graph(const Params<Real> &P0, int grid, int bs) {
+        if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+        if (cudaStreamBeginCapture(ws, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            graph_ok = false;
+            return;
+        }
+        cudaError_t e = enqueue_rounds(P0, grid, bs, false);
         cudaGraph_t g = nullptr;
-        cudaError_t e = cudaStreamEndCapture(ws, &g);
-        if (e != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(e); return EGSGPU_ERR_CUDA; }
-        e = cudaGraphInstantiate(&gexec, g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) { err = std::string("graph instantiate: ") + cudaGetErrorString(e); return EGSGPU_ERR_CUDA; }
-        return 0;
+        cudaError_t e2 = cudaStreamEndCapture(ws, &g);
+        if (e == cudaSuccess && e2 == cudaSuccess && g) e = cudaGraphInstantiate(&gexec, g, 0);
+        else if (e == cudaSuccess) e = e2;
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+            graph_ok = false;
+        }
     }
 
     float elapsed(cudaEvent_t a, cudaEvent_t b) {
@@ -1356,7 +1375,9 @@ struct Engine : EngineBase {
         P.seed = seed;
         P.requeue_lanes = cfg.requeue_lanes > 0 ? cfg.requeue_lanes : 0;
         P.pin = q[0]; P.ein = q[2]; P.pout = q[0]; P.eout = q[2];
-        if (int rc = build_graph(P, grid, bs, err)) return rc;
+        const bool use_graph = cfg.use_graph > 0 && graph_ok;
+        if (use_graph) build_graph(P, grid, bs);
+        const bool graph = use_graph && gexec;
         unsigned *counts = (unsigned *)d_counts.p;
         CK(cudaEventRecord(ev_in, st));
         CK(cudaStreamWaitEvent(ws, ev_in, 0));
@@ -1374,13 +1395,18 @@ struct Engine : EngineBase {
                 unsigned h[9] = {};
                 bool done = false;
                 for (int rep = 0; rep < 100000 / ROUNDS && !done; ++rep) {
-                    CK(cudaGraphLaunch(gexec, ws));
+                    if (graph) CK(cudaGraphLaunch(gexec, ws));
+                    else CK(enqueue_rounds(P, grid, bs, true));
                     CK(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, ws));
                     CK(cudaStreamSynchronize(ws));
                     if (rep == 0) { prof_ms[0] += elapsed(ev[0], ev[1]); ++prof_n[0]; }
                     for (int r = 0; r < ROUNDS; ++r) {
-                        prof_ms[1] += elapsed(gev[4 * r], gev[4 * r + 1]); ++prof_n[1];
-                        prof_ms[2] += elapsed(gev[4 * r + 2], gev[4 * r + 3]); ++prof_n[2];
+                        if (!graph) {
+                            prof_ms[1] += elapsed(gev[4 * r], gev[4 * r + 1]);
+                            prof_ms[2] += elapsed(gev[4 * r + 2], gev[4 * r + 3]);
+                        }
+                        ++prof_n[1];
+                        ++prof_n[2];
                     }
                     if (h[8] > capacity || h[0] > capacity || h[4] > capacity) {
                         err = "particle queue capacity exceeded; lower egsgpu_config.chunk or raise capacity";
@@ -1627,6 +1653,7 @@ int egsgpu_reset(egsgpu_handle *h) {
 }
 
 int egsgpu_get_profile(egsgpu_handle *h, double *out) {
+    // out[16]; see include/egsgpu.h
     if (!h || !out || !h->have_geom) return EGSGPU_ERR_ARG;
     std::string &err = h->err;
     auto get = [&](auto *eng) -> int {
@@ -1637,6 +1664,7 @@ int egsgpu_get_profile(egsgpu_handle *h, double *out) {
         out[10] = (double)c[CNT_PUSH]; out[11] = (double)c[CNT_EPUSH];
         out[12] = (double)c[CNT_INTER]; out[13] = (double)c[CNT_EINTER];
         out[14] = (double)eng->tuned_chunk;
+        out[15] = eng->gexec ? 1.0 : 0.0;
         return 0;
     };
     return h->cfg.precision == 32 ? get((Engine<float> *)h->eng.get()) : get((Engine<double> *)h->eng.get());

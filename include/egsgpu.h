@@ -47,8 +47,10 @@ typedef struct {
     long long chunk;      /* histories per wavefront chunk; 0 = automatic   */
     long long capacity;   /* particle-queue capacity per queue; 0 = automatic */
     int requeue_lanes;    /* a warp whose queue is empty parks its particles for the
-                             next round once this few lanes are busy; 0 = default (8),
-                             -1 = never (results are identical either way) */
+                             next round once this few lanes are busy; <= 0 = never
+                             (default; results are identical either way) */
+    int use_graph;        /* 1: replay the wavefront rounds from a CUDA graph (no
+                             per-kernel timing); 0: direct launches with CUDA events */
 } egsgpu_config;
 
 /* Source: egs++ EGS_ParallelBeam (sources/egs_parallel_beam) with a point
@@ -127,10 +129,11 @@ int egsgpu_get_dose(egsgpu_handle *h, double *dose, double *sigma);
 int egsgpu_set_history_tally(egsgpu_handle *h, long long first, long long n);
 int egsgpu_get_history_tally(egsgpu_handle *h, double *out);
 
-/* Device-side profile of the runs since the last reset: out[15] =
+/* Device-side profile of the runs since the last reset: out[16] =
  * {ms source, ms photon, ms electron, ms batch, launches of each (4),
  *  photon steps, electron steps, photon-kernel pushes, electron-kernel pushes,
- *  photon interactions, electron interactions, autotuned chunk}; times are CUDA-event
+ *  photon interactions, electron interactions, autotuned chunk, graph in use};
+ * times are CUDA-event
  * durations on the launch stream.  No counterpart in the reference API
  * (the reference reports CPU time per batch, egs++/egs_timer.cpp). */
 int egsgpu_get_profile(egsgpu_handle *h, double *out);

@@ -204,6 +204,21 @@ def test_requeue_invariance(precision):
     assert np.allclose(res[0], res[1], rtol=tol, atol=tol)
 
 
+def test_graph_replay_matches_direct_launches():
+    wl = W.slab64(32)
+    n = 20000
+    res = []
+    for g in (0, 1):
+        eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"], precision=64, use_graph=g)
+        eng.set_geometry(wl["geometry"])
+        eng.set_source(wl["source"])
+        eng.set_history_tally(0, n)
+        eng.run(n, nbatch=1, seed=4)
+        res.append(eng.history_tally())
+        assert eng.profile()["graph"] == bool(g)
+    assert np.allclose(res[0], res[1], rtol=1e-12, atol=1e-12)
+
+
 def test_checkpoint_restore_roundtrip():
     wl = W.water30(10)
     eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"])

@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--capacity", type=int, default=0, help="particle-queue capacity (0 = engine default)")
     ap.add_argument("--chunk", type=int, default=0, help="histories per wavefront chunk (0 = automatic)")
+    ap.add_argument("--clock-period", type=float, default=0.2, help="seconds between clock samples")
+    ap.add_argument("--clock-mode", default="nvml", choices=["nvml", "process", "off"])
     return ap.parse_args()
 
 
@@ -71,13 +73,17 @@ class ClockSampler:
     REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
                0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
 
-    def __init__(self, index=0, period=0.2):
+    def __init__(self, index=0, period=0.2, mode="nvml"):
         self.index = index
         self.period = period
+        self.mode = mode
+        self._proc = None
         self.samples = []     # (sm_mhz, max_mhz, reasons_bitmask, power_w)
         self._stop = threading.Event()
         self._t = None
         self._nvml = None
+        if mode != "nvml":
+            return
         try:
             import ctypes
             L = ctypes.CDLL("libnvidia-ml.so.1")
@@ -124,13 +130,32 @@ class ClockSampler:
             self._stop.wait(self.period if self._nvml else 1.0)
 
     def __enter__(self):
+        if self.mode == "off":
+            return self
+        if self.mode == "process":   # nvidia-smi sampling in its own process
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=clocks.sm,clocks.max.sm,"
+                 "clocks_event_reasons.active,power.draw", "--format=csv,noheader,nounits",
+                 "-lms", str(int(1000 * self.period))], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            return self
         self._t = threading.Thread(target=self._run, daemon=True)
         self._t.start()
         return self
 
     def __exit__(self, *a):
-        self._stop.set()
-        self._t.join(timeout=10)
+        if self._proc is not None:
+            self._proc.terminate()
+            out, _ = self._proc.communicate(timeout=10)
+            for line in out.splitlines():
+                f = [x.strip() for x in line.split(",")]
+                try:
+                    self.samples.append((float(f[0]), float(f[1]), int(f[2], 16), float(f[3])))
+                except (ValueError, IndexError):
+                    pass
+            return
+        if self._t is not None:
+            self._stop.set()
+            self._t.join(timeout=10)
 
     def summary(self):
         if not self.samples:
@@ -140,7 +165,7 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(s[1] for s in self.samples),
                 "reasons": reasons, "samples": len(self.samples),
                 "power_w_max": max(s[3] for s in self.samples),
-                "source": "nvml" if self._nvml else "nvidia-smi"}
+                "source": self.mode if self.mode != "nvml" else ("nvml" if self._nvml else "nvidia-smi")}
 
 
 def measured_peak_hbm():
@@ -270,7 +295,7 @@ def main():
     if dist:
         dist.barrier()
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
+    with ClockSampler(local, args.clock_period, args.clock_mode) as clk:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         start.record()

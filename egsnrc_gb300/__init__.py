@@ -69,6 +69,7 @@ def load_library():
     L.egsgpu_get_tallies.argtypes = [vp, dp, dp, dp]
     L.egsgpu_get_dose.argtypes = [vp, dp, dp]
     L.egsgpu_get_profile.argtypes = [vp, dp]
+    L.egsgpu_get_medium.argtypes = [vp, C.c_int, dp]
     L.egsgpu_set_history_tally.argtypes = [vp, i64, i64]
     L.egsgpu_get_history_tally.argtypes = [vp, dp]
     L.egsgpu_checkpoint.argtypes = [vp, vp, C.POINTER(C.c_size_t)]
@@ -169,6 +170,11 @@ class DoseEngine:
         if rc:
             msg = self.L.egsgpu_last_error(self.h if h else None).decode() if h else "create failed"
             raise EGSError(rc, msg)
+
+    def medium(self, index):
+        o = np.zeros(4)
+        self._check(self.L.egsgpu_get_medium(self.h, int(index), _dp(o)))
+        return dict(rho=o[0], ae=o[1], ap=o[2], nelements=int(o[3]))
 
     def set_geometry(self, g):
         self.geom = g

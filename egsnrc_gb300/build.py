@@ -62,7 +62,7 @@ def build_app(force=False):
     if not force and _newer(APP, deps):
         return APP
     _run(["g++", "-O2", "-std=c++17", "-o", APP, src, "-I" + os.path.join(ROOT, "include"),
-          "-L" + HERE, "-legsgpu", "-Wl,-rpath,$ORIGIN"])
+          "-L" + HERE, "-legsgpu", "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + HERE])
     return APP
 
 

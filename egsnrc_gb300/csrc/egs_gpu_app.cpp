@@ -1,0 +1,305 @@
+// egs_gpu_app: runs an egs++ voxel-dose input (EGS_XYZGeometry +
+// EGS_ParallelBeam + EGS_DoseScoring) on the GPU engine through the C ABI.
+//
+//   egs_gpu_app -i input.egsinp -p 521icru [-o name] [--data DIR] [--precision 32|64]
+//
+// It plays the role of an egs++ application built with APP_MAIN
+// (egs++/egs_application.h:1218-1226) for this path: the input blocks are the
+// ones egs_app reads (run control, geometry definition, media, source
+// definition, MC transport parameter, rng definition, ausgab object
+// definition), the PEGS4 file is given with -p, and the dose goes to
+// <name>.3ddose in the egs_dose_scoring format.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <string>
+#include <vector>
+#include <chrono>
+#include <unistd.h>
+#include <libgen.h>
+
+#include "egs_input.h"
+#include "egsgpu.h"
+
+using egsin::Item;
+
+static int fail(const std::string &m) {
+    std::fprintf(stderr, "egs_gpu_app: %s\n", m.c_str());
+    return 1;
+}
+
+static std::string exe_dir() {
+    char buf[4096];
+    ssize_t n = readlink("/proc/self/exe", buf, sizeof(buf) - 1);
+    if (n <= 0) return ".";
+    buf[n] = 0;
+    return std::string(dirname(buf));
+}
+
+struct Phantom {
+    int nx = 0, ny = 0, nz = 0;
+    std::vector<double> xb, yb, zb, rho_abs, rhor;
+    std::vector<int32_t> med;
+    std::vector<std::string> media;
+    bool abs_density = false;
+};
+
+static bool planes(const Item *g, const char *p, const char *s, std::vector<double> &b) {
+    if (g->has(p)) { b = Item::numbers(g->get(p)); return b.size() >= 2; }
+    if (g->has(s)) {   // "x-slabs = first, width, count"
+        auto v = Item::numbers(g->get(s));
+        if (v.size() != 3 || v[2] < 1) return false;
+        b.clear();
+        for (int i = 0; i <= (int)v[2]; ++i) b.push_back(v[0] + i * v[1]);
+        return true;
+    }
+    return false;
+}
+
+static const char *MEDCH = "123456789ABCDEFGHIJKLMNOPQRSTUVWXYZabcdefghijklmnopqrstuvwxyz";
+
+static bool read_egsphant(const std::string &path, Phantom &P, std::string &err) {
+    std::ifstream f(path);
+    if (!f) { err = "cannot open egsphant file " + path; return false; }
+    int nmed;
+    f >> nmed;
+    P.media.resize(nmed);
+    for (auto &m : P.media) f >> m;
+    for (int i = 0; i < nmed; ++i) { double e; f >> e; }
+    f >> P.nx >> P.ny >> P.nz;
+    P.xb.resize(P.nx + 1); P.yb.resize(P.ny + 1); P.zb.resize(P.nz + 1);
+    for (auto &v : P.xb) f >> v;
+    for (auto &v : P.yb) f >> v;
+    for (auto &v : P.zb) f >> v;
+    size_t nv = (size_t)P.nx * P.ny * P.nz;
+    P.med.resize(nv);
+    for (int k = 0; k < P.nz; ++k)
+        for (int j = 0; j < P.ny; ++j) {
+            std::string row;
+            f >> row;
+            if ((int)row.size() < P.nx) { err = "short medium row in " + path; return false; }
+            for (int i = 0; i < P.nx; ++i) {
+                const char *c = std::strchr(MEDCH, row[i]);
+                if (!c || c - MEDCH >= nmed) { err = "bad medium character in " + path; return false; }
+                P.med[(size_t)k * P.nx * P.ny + (size_t)j * P.nx + i] = (int32_t)(c - MEDCH);
+            }
+        }
+    P.rho_abs.resize(nv);
+    for (auto &v : P.rho_abs) f >> v;
+    if (!f) { err = "truncated egsphant file " + path; return false; }
+    P.abs_density = true;
+    return true;
+}
+
+int main(int argc, char **argv) {
+    std::string input, pegs, out, data = exe_dir() + "/data";
+    int precision = 32;
+    for (int i = 1; i < argc; ++i) {
+        std::string a = argv[i];
+        auto next = [&]() { return i + 1 < argc ? std::string(argv[++i]) : std::string(); };
+        if (a == "-i") input = next();
+        else if (a == "-p") pegs = next();
+        else if (a == "-o") out = next();
+        else if (a == "--data") data = next();
+        else if (a == "--precision") precision = std::atoi(next().c_str());
+        else return fail("unknown option " + a);
+    }
+    if (input.empty() || pegs.empty()) return fail("usage: egs_gpu_app -i input -p pegsfile [-o name] [--data dir]");
+    if (input.find('.') == std::string::npos) input += ".egsinp";
+    if (out.empty()) {
+        out = input.substr(0, input.rfind('.'));
+    }
+    std::string pegs_file = pegs;
+    if (pegs_file.find('/') == std::string::npos) pegs_file = data + "/" + pegs_file;
+    if (pegs_file.find(".pegs4dat") == std::string::npos) pegs_file += ".pegs4dat";
+
+    std::string err;
+    auto root = egsin::parse(input, err);
+    if (!root) return fail(err);
+
+    // ---- run control (egs++/egs_run_control.cpp:90-110) ----
+    const Item *rc = root->block("run control");
+    long long ncase = rc ? (long long)rc->num("ncase", 1024) : 1024;
+    int nbatch = rc ? (int)rc->num("nbatch", 10) : 10;
+
+    // ---- transport parameters (egs++/egs_advanced_application.cpp:482-562) ----
+    egsgpu_config cfg;
+    egsgpu_default_config(&cfg);
+    cfg.precision = precision;
+    if (const Item *mc = root->block("MC transport parameter")) {
+        cfg.ecut = mc->num("Global ECUT", cfg.ecut);
+        cfg.pcut = mc->num("Global PCUT", cfg.pcut);
+        cfg.estepe = mc->num("ESTEPE", cfg.estepe);
+        cfg.ximax = mc->num("XImax", cfg.ximax);
+        cfg.skindepth = mc->num("Skin depth for BCA", cfg.skindepth);
+        struct Fixed { const char *key, *value; } fixed[] = {
+            {"Boundary crossing algorithm", "exact"}, {"Electron-step algorithm", "presta-ii"},
+            {"Spin effects", "off"}, {"Brems angular sampling", "km"}, {"Brems cross sections", "bh"},
+            {"Pair angular sampling", "simple"}, {"Pair cross sections", "bh"}, {"Triplet production", "off"},
+            {"Electron impact ionization", "off"}, {"Photonuclear attenuation", "off"},
+            {"Photon cross sections", "xcom"}, {"Bound Compton scattering", "norej"},
+            {"Rayleigh scattering", "on"}, {"Atomic relaxations", "on"}, {"Photoelectron angular sampling", "on"}};
+        for (auto &fx : fixed)
+            if (mc->has(fx.key) && egsin::norm(mc->get(fx.key)) != fx.value)
+                return fail(std::string("'") + fx.key + " = " + mc->get(fx.key) +
+                            "' is not supported (this engine implements " + fx.value + ")");
+    }
+
+    // ---- geometry (EGS_XYZGeometry, egs_nd_geometry.cpp:1160-1260) ----
+    const Item *gd = root->block("geometry definition");
+    if (!gd) return fail("no geometry definition");
+    std::string gname = gd->get("simulation geometry");
+    const Item *g = nullptr;
+    for (auto *b : gd->blocks("geometry"))
+        if (egsin::norm(b->get("name")) == egsin::norm(gname)) g = b;
+    if (!g) return fail("simulation geometry '" + gname + "' not defined");
+    if (egsin::norm(g->get("type")) != "egs_xyzgeometry")
+        return fail("only EGS_XYZGeometry is supported on this path");
+    Phantom P;
+    if (g->has("egsphant file")) {
+        if (!read_egsphant(g->get("egsphant file"), P, err)) return fail(err);
+    } else {
+        if (!planes(g, "x-planes", "x-slabs", P.xb) || !planes(g, "y-planes", "y-slabs", P.yb) ||
+            !planes(g, "z-planes", "z-slabs", P.zb))
+            return fail("XYZ geometry needs x/y/z planes or slabs");
+        P.nx = (int)P.xb.size() - 1; P.ny = (int)P.yb.size() - 1; P.nz = (int)P.zb.size() - 1;
+        size_t nv = (size_t)P.nx * P.ny * P.nz;
+        P.med.assign(nv, 0);
+        P.rhor.assign(nv, 1.0);
+        const Item *mi = g->block("media input");
+        if (!mi) return fail("geometry has no media input");
+        P.media = Item::words(mi->get("media"));
+        // 'set medium = i j', '= i1 i2 j' or '= i1 i2 j step' (egs_base_geometry.cpp:787-811)
+        for (auto &v : mi->all("set medium")) {
+            auto n = Item::numbers(v);
+            int a, b, m, step = 1;
+            if (n.size() == 2) { a = b = (int)n[0]; m = (int)n[1]; }
+            else if (n.size() >= 3) { a = (int)n[0]; b = (int)n[1]; m = (int)n[2]; if (n.size() > 3) step = (int)n[3]; }
+            else return fail("bad 'set medium' input");
+            if (m < 0 || m >= (int)P.media.size()) return fail("'set medium' refers to an undefined medium");
+            for (int r = std::max(a, 0); r <= std::min<long long>(b, (long long)nv - 1); r += std::max(step, 1)) P.med[r] = m;
+        }
+        for (auto &v : mi->all("set relative density")) {
+            auto n = Item::numbers(v);
+            int a = (int)(n[0] + 0.1), b = n.size() == 3 ? (int)(n[1] + 0.1) : a;
+            double r = n.back();
+            for (int k = std::max(a, 0); k <= std::min<long long>(b, (long long)nv - 1); ++k) P.rhor[k] = r;
+        }
+        for (auto &v : g->all("set relative density")) {
+            auto n = Item::numbers(v);
+            int a = (int)(n[0] + 0.1), b = n.size() == 3 ? (int)(n[1] + 0.1) : a;
+            for (int k = std::max(a, 0); k <= std::min<long long>(b, (long long)nv - 1); ++k) P.rhor[k] = n.back();
+        }
+    }
+
+    // ---- engine ----
+    egsgpu_handle *h = nullptr;
+    int st = egsgpu_create(&cfg, &h);
+    if (st) return fail("egsgpu_create failed with status " + std::to_string(st));
+    std::vector<const char *> names;
+    for (auto &m : P.media) names.push_back(m.c_str());
+    if ((st = egsgpu_load_media(h, data.c_str(), pegs_file.c_str(), names.data(), (int)names.size())))
+        return fail(egsgpu_last_error(h));
+    if (P.abs_density) {   // relative density = mass density / PEGS4 density
+        P.rhor.resize(P.rho_abs.size());
+        for (size_t i = 0; i < P.rho_abs.size(); ++i) {
+            double info[4];
+            egsgpu_get_medium(h, P.med[i], info);
+            P.rhor[i] = P.rho_abs[i] / info[0];
+        }
+    }
+    if ((st = egsgpu_set_xyz_geometry(h, P.nx, P.ny, P.nz, P.xb.data(), P.yb.data(), P.zb.data(), P.med.data(),
+                                      P.rhor.data())))
+        return fail(egsgpu_last_error(h));
+
+    // ---- source (EGS_ParallelBeam; egs_base_source.cpp:46, egs_parallel_beam.cpp:43) ----
+    const Item *sd = root->block("source definition");
+    if (!sd) return fail("no source definition");
+    std::string sname = sd->get("simulation source");
+    const Item *s = nullptr;
+    for (auto *b : sd->blocks("source"))
+        if (egsin::norm(b->get("name")) == egsin::norm(sname)) s = b;
+    if (!s) return fail("simulation source '" + sname + "' not defined");
+    if (egsin::norm(s->get("library")) != "egs_parallel_beam") return fail("only egs_parallel_beam sources are supported");
+    egsgpu_source src;
+    std::memset(&src, 0, sizeof(src));
+    src.charge = (int)s->num("charge", 0);
+    auto dir = Item::numbers(s->get("direction", "0 0 1"));
+    for (int k = 0; k < 3; ++k) src.dir[k] = k < (int)dir.size() ? dir[k] : 0;
+    const Item *sh = s->block("shape");
+    if (!sh) return fail("source has no shape");
+    std::string stype = egsin::norm(sh->get("type"));
+    double tr[3] = {0, 0, 0};
+    if (const Item *t = sh->block("transformation")) {
+        auto v = Item::numbers(t->get("translation", "0 0 0"));
+        for (int k = 0; k < 3 && k < (int)v.size(); ++k) tr[k] = v[k];
+    }
+    if (stype == "point") {
+        auto p = Item::numbers(sh->get("position", "0 0 0"));
+        src.shape = 0;
+        for (int k = 0; k < 3; ++k) src.pos[k] = (k < (int)p.size() ? p[k] : 0) + tr[k];
+    } else if (stype == "rectangle") {
+        auto r = Item::numbers(sh->get("rectangle"));
+        if (r.size() != 4) return fail("rectangle needs x1 y1 x2 y2");
+        src.shape = 1;
+        src.xmin = std::min(r[0], r[2]) + tr[0]; src.xmax = std::max(r[0], r[2]) + tr[0];
+        src.ymin = std::min(r[1], r[3]) + tr[1]; src.ymax = std::max(r[1], r[3]) + tr[1];
+        src.pos[2] = tr[2];
+    } else return fail("shape type '" + sh->get("type") + "' is not supported");
+    const Item *sp = s->block("spectrum");
+    if (!sp) return fail("source has no spectrum");
+    std::vector<double> edges, weights;
+    std::string sptype = egsin::norm(sp->get("type"));
+    if (sptype == "monoenergetic") {
+        src.spectrum = 0;
+        src.energy = sp->num("energy", 0);
+    } else if (sptype == "tabulated spectrum") {
+        edges = Item::numbers(sp->get("energies"));
+        weights = Item::numbers(sp->get("probabilities"));
+        int mode = (int)sp->num("spectrum mode", sp->num("spectrum type", 1));
+        if (mode != 1 || edges.size() != weights.size() + 1 || weights.empty())
+            return fail("tabulated spectra must be histograms (mode 1: N+1 energies, N probabilities)");
+        src.spectrum = 1;
+        src.nbins = (int)weights.size();
+        src.edges = edges.data();
+        src.weights = weights.data();
+    } else return fail("spectrum type '" + sp->get("type") + "' is not supported");
+    if ((st = egsgpu_set_source(h, &src))) return fail(egsgpu_last_error(h));
+
+    uint32_t seed = 1;
+    if (const Item *rng = root->block("rng definition")) {
+        auto v = Item::numbers(rng->get("initial seeds", "1"));
+        if (!v.empty()) seed = (uint32_t)v[0];
+    }
+
+    auto t0 = std::chrono::steady_clock::now();
+    if ((st = egsgpu_run(h, 0, ncase, nbatch, seed, nullptr))) return fail(egsgpu_last_error(h));
+    double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+
+    size_t nv = (size_t)P.nx * P.ny * P.nz;
+    std::vector<double> dose(nv), sig(nv);
+    double tot[8];
+    egsgpu_get_dose(h, dose.data(), sig.data());
+    egsgpu_get_tallies(h, nullptr, nullptr, tot);
+    std::printf("histories %lld in %d batches, %.3f s (%.4g histories/s)\n", ncase, nbatch, dt, ncase / dt);
+    std::printf("deposited %.6g MeV, escaped %.6g MeV per history\n", tot[2] / ncase, tot[3] / ncase);
+
+    // .3ddose (egs_dose_scoring.cpp:416-480)
+    std::string fn = out + ".3ddose";
+    FILE *f = std::fopen(fn.c_str(), "w");
+    if (!f) return fail("cannot write " + fn);
+    std::fprintf(f, "%d %d %d\n", P.nx, P.ny, P.nz);
+    for (auto *b : {&P.xb, &P.yb, &P.zb}) {
+        for (double v : *b) std::fprintf(f, "%g ", (float)v);
+        std::fprintf(f, "\n");
+    }
+    for (size_t i = 0; i < nv; ++i) std::fprintf(f, "%g ", (float)dose[i]);
+    std::fprintf(f, "\n");
+    for (size_t i = 0; i < nv; ++i) std::fprintf(f, "%g ", (float)(dose[i] > 0 ? sig[i] / dose[i] : 1.0));
+    std::fprintf(f, "\n");
+    std::fclose(f);
+    std::printf("wrote %s\n", fn.c_str());
+    egsgpu_destroy(h);
+    return 0;
+}

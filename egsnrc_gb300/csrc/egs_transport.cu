@@ -1539,6 +1539,15 @@ int egsgpu_load_media(egsgpu_handle *h, const char *data_dir, const char *pegs_f
     return 0;
 }
 
+int egsgpu_get_medium(egsgpu_handle *h, int index, double *out) {
+    if (!h || !out) return EGSGPU_ERR_ARG;
+    if (!h->have_media) { h->err = "no media loaded"; return EGSGPU_ERR_STATE; }
+    if (index < 0 || index >= (int)h->H.media.size()) { h->err = "medium index out of range"; return EGSGPU_ERR_ARG; }
+    const egs::Medium &m = h->H.media[index];
+    out[0] = m.rho; out[1] = m.ae; out[2] = m.ap; out[3] = m.nne;
+    return 0;
+}
+
 int egsgpu_set_xyz_geometry(egsgpu_handle *h, int nx, int ny, int nz, const double *xb, const double *yb,
                             const double *zb, const int32_t *med, const double *rhor) {
     if (!h || nx < 1 || ny < 1 || nz < 1 || !xb || !yb || !zb || !med || !rhor) return EGSGPU_ERR_ARG;

@@ -84,6 +84,11 @@ int egsgpu_create(const egsgpu_config *cfg, egsgpu_handle **out);
 int egsgpu_load_media(egsgpu_handle *h, const char *data_dir, const char *pegs_file,
                       const char *const *names, int n);
 
+/* Properties of loaded medium `index`: out[4] = {PEGS4 density (g/cm^3),
+ * AE, AP (MeV), number of elements}. Replaces reading the MEDIA/THRESH
+ * COMMON blocks (interface/egs_interface2.h:108-692: the_media, the_thresh). */
+int egsgpu_get_medium(egsgpu_handle *h, int index, double *out);
+
 /* Voxel phantom: plane positions (nx+1, ny+1, nz+1, cm), medium index and
  * relative density per voxel, voxel index ix + iy*nx + iz*nx*ny.
  * Replaces EGS_XYZGeometry construction and the egsHowfar/egsHownear/

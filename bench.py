@@ -285,6 +285,8 @@ def main():
     eng.set_geometry(wl["geometry"])
     eng.set_source(wl["source"])
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    flush.zero_()   # loads torch's fill kernel before anything is timed
+    torch.cuda.synchronize()
     base = rank * (K + Wm + 2) * H     # disjoint history ranges per rank
     first = base
     for _ in range(Wm):

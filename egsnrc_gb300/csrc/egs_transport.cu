@@ -71,6 +71,7 @@ struct Params {
 // this few of its lanes are still busy (only when the launch is large enough
 // for the next round to refill warps).
 constexpr unsigned REQUEUE_MIN = 32768;
+constexpr int LSTACK = 6;   // per-thread LIFO depth for charged secondaries
 
 // ------------------------------------------------------------- tallies ----
 template <class Real>
@@ -546,6 +547,12 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
     Particle<Real> p;
     ElecState<Real> s;
     Real edep_part = 0;   // continuous-loss deposits of the current particle
+    // EGSnrc's own stack discipline for the charged secondaries of Moller and
+    // Bhabha events: the primary is suspended on a small per-thread LIFO (in
+    // local memory) and the secondary is followed first; a full stack spills
+    // to the next electron queue.
+    Particle<Real> lstack[LSTACK];
+    int sp = 0;
     Acc<Real> acc{-1, 0u, (Real)0};
     bool alive = false, exhausted = false;
     unsigned long long nstep = 0, npush = 0, ninter = 0;
@@ -554,9 +561,18 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
     const Real rm = (Real)RM;
     const bool requeue = P.requeue_lanes > 0 && nq >= REQUEUE_MIN;
     while (true) {
+        if (!alive && sp > 0) {   // resume a suspended particle
+            p = lstack[--sp];
+            alive = true;
+            s.state = 0;
+            s.nsteps = 0;
+            s.medium = G.med[p.ir];
+            s.rhor = G.rhor[p.ir];
+        }
         if (exhausted && requeue) {
             unsigned busy = __ballot_sync(0xffffffffu, alive);
             if (__popc(busy) <= P.requeue_lanes) {   // park the survivors and retire the warp
+                while (sp > 0) q_push(P, P.eout, lstack[--sp], npush);
                 if (alive) {
                     unsigned i = q_slot(P, P.eout);
                     if (i != ~0u) {
@@ -822,7 +838,8 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                                 costhe = dsqrt(dmin((Real)1, dcosth));
                                 rotate(a, b, c, sinthe, costhe, az, d.u, d.v, d.w);
                                 d.E = pese2; d.iq = -1;
-                                push_charged(P, P.eout, P.pout, d, acc, npush, edep_tot, err);
+                                if (d.E > T.ecut && sp < LSTACK) { lstack[sp++] = p; p = d; }
+                                else push_charged(P, P.eout, P.pout, d, acc, npush, edep_tot, err);
                                 s.state = 0;
                                 continue;
                             }
@@ -863,7 +880,8 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                                     costhe = dsqrt(dmin((Real)1, dcosth));
                                     rotate(a, b, c, sinthe, costhe, az, d.u, d.v, d.w);
                                     d.E = pese2; d.iq = iq_new;
-                                    push_charged(P, P.eout, P.pout, d, acc, npush, edep_tot, err);
+                                    if (d.E > T.ecut && sp < LSTACK) { lstack[sp++] = p; p = d; }
+                                    else push_charged(P, P.eout, P.pout, d, acc, npush, edep_tot, err);
                                     s.state = 0;
                                     continue;
                                 }
@@ -1361,7 +1379,11 @@ struct Engine : EngineBase {
             chunk = tuned_chunk;
         }
         const int bs = cfg.block_size > 0 ? cfg.block_size : 128;
-        const int cps = cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm : 8;
+        // persistent grids: never more CTAs than can be resident at once
+        int occ_p = 1, occ_e = 1;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real>, bs, 0));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real>, bs, 0));
+        const int cps = std::max(1, std::min(cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm : 64, std::min(occ_p, occ_e)));
         const int grid = sm_count * cps;
         Params<Real> P;
         P.T = T; P.G = G;

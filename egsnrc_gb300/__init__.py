@@ -211,14 +211,14 @@ class DoseEngine:
         return d, s
 
     def profile(self):
-        o = np.zeros(16)
+        o = np.zeros(18)
         self._check(self.L.egsgpu_get_profile(self.h, _dp(o)))
         keys = ("source", "photon", "electron", "batch")
         d = {"ms_" + k: o[i] for i, k in enumerate(keys)}
         d.update({"launches_" + k: int(o[4 + i]) for i, k in enumerate(keys)})
         d.update(photon_steps=o[8], electron_steps=o[9], photon_pushes=o[10], electron_pushes=o[11],
                  photon_interactions=o[12], electron_interactions=o[13], chunk=int(o[14]),
-                 graph=bool(o[15]))
+                 graph=bool(o[15]), photon_busy_lanes=o[16], electron_busy_lanes=o[17])
         return d
 
     def set_history_tally(self, first, n):

@@ -120,6 +120,11 @@ __host__ __device__ inline uint64_t child_sid(uint64_t sid, uint32_t n, uint32_t
     return mix64(sid + 0x9E3779B97F4A7C15ull * (1 + (((uint64_t)n) << 3) + k));
 }
 
+// One Philox block, kept out of line: the generator is called from about a
+// hundred places in the transport kernels and inlining its ten rounds at each
+// would multiply the kernels' instruction footprint.
+__device__ __noinline__ uint4 philox_block(uint32_t b, uint32_t s0, uint32_t s1, uint32_t k0, uint32_t k1);
+
 struct Rng {
     uint32_t seed, hist, n, blk;
     uint64_t sid;
@@ -130,9 +135,8 @@ struct Rng {
     __device__ float u() {
         uint32_t b = n >> 2;
         if (b != blk) {
-            uint32_t o[4];
-            philox10(b, (uint32_t)sid, (uint32_t)(sid >> 32), 0u, seed, hist, o);
-            c0 = o[0]; c1 = o[1]; c2 = o[2]; c3 = o[3];
+            uint4 o = philox_block(b, (uint32_t)sid, (uint32_t)(sid >> 32), seed, hist);
+            c0 = o.x; c1 = o.y; c2 = o.z; c3 = o.w;
             blk = b;
         }
         uint32_t j = n & 3u, x = (j == 0) ? c0 : (j == 1) ? c1 : (j == 2) ? c2 : c3;

@@ -38,6 +38,12 @@ namespace cg = cooperative_groups;
 
 namespace egsgpu {
 
+__device__ __noinline__ uint4 philox_block(uint32_t b, uint32_t s0, uint32_t s1, uint32_t k0, uint32_t k1) {
+    uint32_t o[4];
+    philox10(b, s0, s1, 0u, k0, k1, o);
+    return make_uint4(o[0], o[1], o[2], o[3]);
+}
+
 __constant__ MedScalars<float> c_med_f[MAXMED];
 __constant__ MedScalars<double> c_med_d[MAXMED];
 template <class Real> __device__ inline const MedScalars<Real> &cmed(int m);
@@ -49,7 +55,8 @@ template <> __device__ inline const MedScalars<double> &cmed<double>(int m) { re
 // (EGSGPU_ERR_LOOP); no physical history comes near it.
 constexpr int STEP_CAP = 1 << 22;
 
-enum { CNT_PSTEP = 0, CNT_ESTEP = 1, CNT_PUSH = 2, CNT_INTER = 3, CNT_EPUSH = 4, CNT_EINTER = 5, CNT_N = 8 };
+enum { CNT_PSTEP = 0, CNT_ESTEP = 1, CNT_PUSH = 2, CNT_INTER = 3, CNT_EPUSH = 4, CNT_EINTER = 5,
+       CNT_PLANES = 6, CNT_PITER = 7, CNT_ELANES = 8, CNT_EITER = 9, CNT_N = 12 };
 
 template <class Real>
 struct Params {
@@ -320,7 +327,7 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
     PhotonState<Real> s;
     Acc<Real> acc{-1, 0u, (Real)0};
     bool alive = false, exhausted = false;
-    unsigned long long nstep = 0, npush = 0, ninter = 0;
+    unsigned long long nstep = 0, npush = 0, ninter = 0, lanes = 0, iters = 0;
     double edep_tot = 0, esc_tot = 0;
     int err = 0;
     const Real rm = (Real)RM;
@@ -362,7 +369,10 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
                 }
             }
         }
-        if (!__any_sync(0xffffffffu, alive)) break;
+        unsigned live = __ballot_sync(0xffffffffu, alive);
+        if (!live) break;
+        lanes += __popc(live);
+        ++iters;
         if (!alive) continue;
 
         if (s.state == 0) {   // :PNEWENERGY:
@@ -458,6 +468,8 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
         esc_tot += __shfl_down_sync(0xffffffffu, esc_tot, o);
     }
     if (lane == 0) {
+        atomicAdd(P.counters + CNT_PLANES, lanes);
+        atomicAdd(P.counters + CNT_PITER, iters);
         atomicAdd(P.counters + CNT_PSTEP, nstep);
         atomicAdd(P.counters + CNT_PUSH, npush);
         atomicAdd(P.counters + CNT_INTER, ninter);
@@ -555,7 +567,7 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
     int sp = 0;
     Acc<Real> acc{-1, 0u, (Real)0};
     bool alive = false, exhausted = false;
-    unsigned long long nstep = 0, npush = 0, ninter = 0;
+    unsigned long long nstep = 0, npush = 0, ninter = 0, lanes = 0, iters = 0;
     double edep_tot = 0, esc_tot = 0;
     int err = 0;
     const Real rm = (Real)RM;
@@ -620,7 +632,10 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                 }
             }
         }
-        if (!__any_sync(0xffffffffu, alive)) break;
+        unsigned live = __ballot_sync(0xffffffffu, alive);
+        if (!live) break;
+        lanes += __popc(live);
+        ++iters;
         if (!alive) continue;
 
         const int qel = (1 + p.iq) / 2;
@@ -1009,6 +1024,8 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
         esc_tot += __shfl_down_sync(0xffffffffu, esc_tot, o);
     }
     if (lane == 0) {
+        atomicAdd(P.counters + CNT_ELANES, lanes);
+        atomicAdd(P.counters + CNT_EITER, iters);
         atomicAdd(P.counters + CNT_ESTEP, nstep);
         atomicAdd(P.counters + CNT_EPUSH, npush);
         atomicAdd(P.counters + CNT_EINTER, ninter);
@@ -1406,8 +1423,8 @@ struct Engine : EngineBase {
         long long per_batch = n / nbatch;
         for (int b = 0; b < nbatch; ++b) {
             long long b0 = first + b * per_batch, bn = (b == nbatch - 1) ? n - b * per_batch : per_batch;
-            for (long long c0 = b0; c0 < b0 + bn; c0 += chunk) {
-                long long cn = std::min(chunk, b0 + bn - c0);
+            for (long long c0 = b0, cn = 0; c0 < b0 + bn; c0 += cn) {
+                cn = std::min(chunk, b0 + bn - c0);   // the autotuner may change `chunk` below
                 auto t_chunk = std::chrono::steady_clock::now();
                 CK(cudaMemsetAsync(counts, 0, 9 * sizeof(unsigned), ws));
                 CK(cudaEventRecord(ev[0], ws));
@@ -1684,7 +1701,7 @@ int egsgpu_reset(egsgpu_handle *h) {
 }
 
 int egsgpu_get_profile(egsgpu_handle *h, double *out) {
-    // out[16]; see include/egsgpu.h
+    // out[18]; see include/egsgpu.h
     if (!h || !out || !h->have_geom) return EGSGPU_ERR_ARG;
     std::string &err = h->err;
     auto get = [&](auto *eng) -> int {
@@ -1696,6 +1713,8 @@ int egsgpu_get_profile(egsgpu_handle *h, double *out) {
         out[12] = (double)c[CNT_INTER]; out[13] = (double)c[CNT_EINTER];
         out[14] = (double)eng->tuned_chunk;
         out[15] = eng->gexec ? 1.0 : 0.0;
+        out[16] = c[CNT_PITER] ? (double)c[CNT_PLANES] / c[CNT_PITER] : 0.0;
+        out[17] = c[CNT_EITER] ? (double)c[CNT_ELANES] / c[CNT_EITER] : 0.0;
         return 0;
     };
     return h->cfg.precision == 32 ? get((Engine<float> *)h->eng.get()) : get((Engine<double> *)h->eng.get());

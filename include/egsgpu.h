@@ -134,10 +134,11 @@ int egsgpu_get_dose(egsgpu_handle *h, double *dose, double *sigma);
 int egsgpu_set_history_tally(egsgpu_handle *h, long long first, long long n);
 int egsgpu_get_history_tally(egsgpu_handle *h, double *out);
 
-/* Device-side profile of the runs since the last reset: out[16] =
+/* Device-side profile of the runs since the last reset: out[18] =
  * {ms source, ms photon, ms electron, ms batch, launches of each (4),
  *  photon steps, electron steps, photon-kernel pushes, electron-kernel pushes,
- *  photon interactions, electron interactions, autotuned chunk, graph in use};
+ *  photon interactions, electron interactions, autotuned chunk, graph in use,
+ *  mean busy lanes per warp iteration in the photon and electron kernels};
  * times are CUDA-event
  * durations on the launch stream.  No counterpart in the reference API
  * (the reference reports CPU time per batch, egs++/egs_timer.cpp). */

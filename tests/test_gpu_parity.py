@@ -168,6 +168,28 @@ def test_energy_conservation(precision):
     assert abs(s.sum() - t["deposited"]) < (1e-9 if precision == 64 else 1e-6) * t["deposited"]
 
 
+def test_autotuned_chunks_cover_every_history():
+    # a small queue capacity makes the autotuner start with tiny chunks and
+    # grow them many times within one batch; every history must be run once
+    wl = W.water30(10)
+    n = 60000
+    eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"], precision=64, capacity=1 << 15)
+    eng.set_geometry(wl["geometry"])
+    eng.set_source(wl["source"])
+    eng.set_history_tally(0, n)
+    eng.run(n, nbatch=3, seed=8)
+    t = eng.totals()
+    assert t["histories"] == n
+    assert abs(t["deposited"] + t["escaped"] - 2.0 * n) < 1e-8 * n
+    ref = eg.DoseEngine(wl["media"], ecut=wl["ecut"], precision=64, chunk=n)
+    ref.set_geometry(wl["geometry"])
+    ref.set_source(wl["source"])
+    ref.set_history_tally(0, n)
+    ref.run(n, nbatch=3, seed=8)
+    assert np.allclose(eng.history_tally(), ref.history_tally(), rtol=1e-12, atol=1e-12)
+    assert eng.profile()["chunk"] > 2000
+
+
 @pytest.mark.parametrize("precision", [32, 64])
 def test_chunking_invariance(precision):
     wl = W.water30(20)

@@ -72,6 +72,7 @@ struct Params {
     unsigned *peak;                       // largest queue length seen (autotuner input)
     uint32_t seed;
     int requeue_lanes;                    // park survivors of warps this sparse (0 = never)
+    int inter_batch;                      // lanes due to interact before the warp samples them
 };
 
 // A warp whose queue is exhausted parks its particles in the next queue once
@@ -79,6 +80,7 @@ struct Params {
 // for the next round to refill warps).
 constexpr unsigned REQUEUE_MIN = 32768;
 constexpr int LSTACK = 6;   // per-thread LIFO depth for charged secondaries
+constexpr int INTER_MAXWAIT = 24;   // longest wait of a lane due to interact
 
 // ------------------------------------------------------------- tallies ----
 template <class Real>
@@ -328,6 +330,7 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
     Acc<Real> acc{-1, 0u, (Real)0};
     bool alive = false, exhausted = false;
     unsigned long long nstep = 0, npush = 0, ninter = 0, lanes = 0, iters = 0;
+    int inter_wait = 0;   // warp-uniform iterations since the first lane became due
     double edep_tot = 0, esc_tot = 0;
     int err = 0;
     const Real rm = (Real)RM;
@@ -340,7 +343,8 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
                     unsigned i = q_slot(P, P.pout);
                     if (i != ~0u) {
                         q_store(P.pout, i, p);
-                        if (s.state != 0) { P.pout.st[i] = 1; P.pout.aux0[i] = s.dpmfp; }
+                        if (s.state == 3) P.pout.st[i] = 3;
+                        else if (s.state != 0) { P.pout.st[i] = 1; P.pout.aux0[i] = s.dpmfp; }
                     }
                 }
                 break;
@@ -359,7 +363,16 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
                     alive = true;
                     s.state = 0;
                     s.nsteps = 0;
-                    if (P.pin.st[idx]) {   // resume a parked photon
+                    if (P.pin.st[idx] == 3) {   // resume a photon due to interact
+                        const MedScalars<Real> &M = cmed<Real>(G.med[p.ir]);
+                        s.state = 3;
+                        s.medium = G.med[p.ir];
+                        s.rhor = G.rhor[p.ir];
+                        s.gle = dlog(p.E);
+                        s.lgle = min(max((int)(M.ge1 * s.gle + M.ge0), 1), MXGE);
+                        const Real *g = T.gtab + ((size_t)M.gtab_off + s.lgle - 1) * 8;
+                        s.cohfac = g[7] * s.gle + g[6];
+                    } else if (P.pin.st[idx]) {   // resume a parked photon
                         s.state = 1;
                         s.medium = G.med[p.ir];
                         s.rhor = G.rhor[p.ir];
@@ -373,7 +386,67 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
         if (!live) break;
         lanes += __popc(live);
         ++iters;
-        if (!alive) continue;
+        // Interactions are sampled for several lanes at once: a lane whose
+        // photon is due to interact waits until enough of the warp is due too
+        // (or a bounded number of iterations has passed).
+        {
+            unsigned pend = __ballot_sync(0xffffffffu, alive && s.state == 3);
+            bool batch = false;
+            if (pend) {
+                ++inter_wait;
+                batch = __popc(pend) >= min(P.inter_batch, __popc(live)) || inter_wait > INTER_MAXWAIT;
+            }
+            if (batch) {
+                inter_wait = 0;
+                if (alive && s.state == 3) {
+                // interaction
+                ++ninter;
+                const MedScalars<Real> &M = cmed<Real>(s.medium);
+                const Real *g = T.gtab + ((size_t)M.gtab_off + s.lgle - 1) * 8;
+                Real r37 = urand<Real>(p.rng);
+                if (r37 <= 1 - s.cohfac) {   // Rayleigh (src/egsnrc.macros:1602-1613)
+                    Real costhe, sinthe;
+                    rayleigh(T, s.medium, p.E, s.gle, s.lgle, p.rng, costhe, sinthe, err);
+                    Azim<Real> az = azimuth<Real>(p.rng, err);
+                    Real a = p.u, b = p.v, c = p.w;
+                    rotate(a, b, c, sinthe, costhe, az, p.u, p.v, p.w);
+                    s.state = 0;
+                    continue;
+                }
+                Real r36 = urand<Real>(p.rng);
+                Real gbr1 = g[3] * s.gle + g[2];
+                if (r36 <= gbr1 && p.E > 2 * rm) {
+                    Real E2, u2, v2, w2;
+                    int iq2;
+                    pair(M, p, E2, iq2, u2, v2, w2, err);
+                    Particle<Real> q = p;
+                    q.E = E2; q.iq = iq2; q.u = u2; q.v = v2; q.w = w2;
+                    q.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
+                    push_charged(P, P.ein, P.pout, p, acc, npush, edep_tot, err);
+                    push_charged(P, P.ein, P.pout, q, acc, npush, edep_tot, err);
+                    alive = false;
+                    continue;
+                }
+                Real gbr2 = g[5] * s.gle + g[4];
+                if (r36 < gbr2) {
+                    Particle<Real> e = p;
+                    Real edep = compton(T, M, p, e.u, e.v, e.w, e.E, err);
+                    e.iq = -1;
+                    e.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
+                    if (edep > 0) { deposit(P, acc, p.ir, p.rng.hist, edep * p.wt); edep_tot += (double)(edep * p.wt); }
+                    push_charged(P, P.ein, P.pout, e, acc, npush, edep_tot, err);
+                    s.state = 0;
+                    continue;
+                }
+                Real edep = photo(T, M, p, s.gle, err);
+                if (edep > 0) { deposit(P, acc, p.ir, p.rng.hist, edep * p.wt); edep_tot += (double)(edep * p.wt); }
+                push_charged(P, P.ein, P.pout, p, acc, npush, edep_tot, err);
+                alive = false;
+                }
+                continue;
+            }
+        }
+        if (!alive || s.state == 3) continue;
 
         if (s.state == 0) {   // :PNEWENERGY:
             if (p.E <= T.pcut) {   // :PCUT-DISCARD:
@@ -414,49 +487,7 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
         }
         if (s.dpmfp > (Real)1e-8) continue;
 
-        // interaction
-        ++ninter;
-        const MedScalars<Real> &M = cmed<Real>(s.medium);
-        const Real *g = T.gtab + ((size_t)M.gtab_off + s.lgle - 1) * 8;
-        Real r37 = urand<Real>(p.rng);
-        if (r37 <= 1 - s.cohfac) {   // Rayleigh (src/egsnrc.macros:1602-1613)
-            Real costhe, sinthe;
-            rayleigh(T, s.medium, p.E, s.gle, s.lgle, p.rng, costhe, sinthe, err);
-            Azim<Real> az = azimuth<Real>(p.rng, err);
-            Real a = p.u, b = p.v, c = p.w;
-            rotate(a, b, c, sinthe, costhe, az, p.u, p.v, p.w);
-            s.state = 0;
-            continue;
-        }
-        Real r36 = urand<Real>(p.rng);
-        Real gbr1 = g[3] * s.gle + g[2];
-        if (r36 <= gbr1 && p.E > 2 * rm) {
-            Real E2, u2, v2, w2;
-            int iq2;
-            pair(M, p, E2, iq2, u2, v2, w2, err);
-            Particle<Real> q = p;
-            q.E = E2; q.iq = iq2; q.u = u2; q.v = v2; q.w = w2;
-            q.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
-            push_charged(P, P.ein, P.pout, p, acc, npush, edep_tot, err);
-            push_charged(P, P.ein, P.pout, q, acc, npush, edep_tot, err);
-            alive = false;
-            continue;
-        }
-        Real gbr2 = g[5] * s.gle + g[4];
-        if (r36 < gbr2) {
-            Particle<Real> e = p;
-            Real edep = compton(T, M, p, e.u, e.v, e.w, e.E, err);
-            e.iq = -1;
-            e.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
-            if (edep > 0) { deposit(P, acc, p.ir, p.rng.hist, edep * p.wt); edep_tot += (double)(edep * p.wt); }
-            push_charged(P, P.ein, P.pout, e, acc, npush, edep_tot, err);
-            s.state = 0;
-            continue;
-        }
-        Real edep = photo(T, M, p, s.gle, err);
-        if (edep > 0) { deposit(P, acc, p.ir, p.rng.hist, edep * p.wt); edep_tot += (double)(edep * p.wt); }
-        push_charged(P, P.ein, P.pout, p, acc, npush, edep_tot, err);
-        alive = false;
+        s.state = 3;   // interaction due: wait for the warp's batch
     }
     acc_flush(P, acc);
     // block-level counter reduction via warp shuffles
@@ -568,6 +599,7 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
     Acc<Real> acc{-1, 0u, (Real)0};
     bool alive = false, exhausted = false;
     unsigned long long nstep = 0, npush = 0, ninter = 0, lanes = 0, iters = 0;
+    int inter_wait = 0;   // warp-uniform iterations since the first lane became due
     double edep_tot = 0, esc_tot = 0;
     int err = 0;
     const Real rm = (Real)RM;
@@ -590,6 +622,7 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                     if (i != ~0u) {
                         q_store(P.eout, i, p);
                         if (s.state == 1) P.eout.st[i] = 1;
+                        else if (s.state == 3) P.eout.st[i] = 8;
                         else if (s.state == 2) {
                             P.eout.st[i] = (uint8_t)(2 | (s.compute_tstep ? 4 : 0));
                             P.eout.aux0[i] = s.demfp; P.eout.aux1[i] = s.total_de;
@@ -619,6 +652,13 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                     s.rhor = G.rhor[p.ir];
                     uint8_t st = P.ein.st[idx];
                     if (st == 1) s.state = 1;
+                    else if (st == 8) {   // resume a particle due to interact
+                        const MedScalars<Real> &M = cmed<Real>(s.medium);
+                        s.state = 3;
+                        s.eke = p.E - (Real)RM;
+                        s.elke = dlog(s.eke);
+                        s.lelke = min(max((int)(M.eke1 * s.elke + M.eke0), 1), M.meke);
+                    }
                     else if (st & 2) {   // resume a parked condensed-history sequence
                         const MedScalars<Real> &M = cmed<Real>(s.medium);
                         s.state = 2;
@@ -636,7 +676,216 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
         if (!live) break;
         lanes += __popc(live);
         ++iters;
-        if (!alive) continue;
+        // Discrete interactions are sampled for several lanes at once (see the
+        // photon kernel).
+        {
+            unsigned pend = __ballot_sync(0xffffffffu, alive && s.state == 3);
+            bool batch = false;
+            if (pend) {
+                ++inter_wait;
+                batch = __popc(pend) >= min(P.inter_batch, __popc(live)) || inter_wait > INTER_MAXWAIT;
+            }
+            if (batch) {
+                inter_wait = 0;
+                if (alive && s.state == 3) {
+                const int qel = (1 + p.iq) / 2;
+                const MedScalars<Real> &M2 = cmed<Real>(s.medium);
+                ERow<Real> ef{erow(T, M2, s.lelke), qel};
+                    // discrete interaction
+                    ++ninter;
+                    const Real *rw = ef.r;
+                    bool brems = false;
+                    if (p.iq < 0) {
+                        Real ebr1 = rw[9] * s.elke + rw[8];
+                        Real r24 = urand<Real>(p.rng);
+                        brems = r24 <= ebr1;
+                        if (!brems && p.E <= M2.thmoll) {
+                            if (ebr1 <= 0) { s.state = 0; continue; }
+                            brems = true;
+                        }
+                        if (!brems) {   // MOLLER (src/egsnrc.mortran:2599-2746)
+                            Real peie = p.E, ekin = peie - rm;
+                            if (ekin <= 2 * M2.te) { s.state = 0; continue; }
+                            Real t0 = ekin / rm, e0 = t0 + 1, extrae = peie - M2.thmoll, e02 = e0 * e0;
+                            Real g2 = t0 * t0 / e02, g3 = (2 * t0 + 1) / e02, gmax = 1 + (Real)1.25 * g2, br, rejf4, r28;
+                            int it = 0;
+                            do {
+                                Real r27 = urand<Real>(p.rng);
+                                br = M2.te / (ekin - extrae * r27);
+                                Real rr2 = br / (1 - br);
+                                r28 = urand<Real>(p.rng);
+                                rejf4 = 1 + g2 * br * br + rr2 * (rr2 - g3);
+                                r28 = gmax * r28;
+                                if (++it > LOOP_CAP) { err = 1; break; }
+                            } while (!(r28 <= rejf4));
+                            Real pekse2 = br * ekin, pese1 = peie - pekse2, pese2 = pekse2 + rm;
+                            Real h1 = (peie + rm) / ekin;
+                            Real dcosth = h1 * (pese1 - rm) / (pese1 + rm);
+                            Real sinthe = dsqrt(dmax((Real)0, 1 - dcosth)), costhe = dsqrt(dmin((Real)1, dcosth));
+                            Azim<Real> az = azimuth<Real>(p.rng, err);
+                            Real a = p.u, b = p.v, c = p.w;
+                            rotate(a, b, c, sinthe, costhe, az, p.u, p.v, p.w);
+                            p.E = pese1;
+                            Particle<Real> d = p;
+                            d.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
+                            dcosth = h1 * (pese2 - rm) / (pese2 + rm);
+                            sinthe = -dsqrt(dmax((Real)0, 1 - dcosth));
+                            costhe = dsqrt(dmin((Real)1, dcosth));
+                            rotate(a, b, c, sinthe, costhe, az, d.u, d.v, d.w);
+                            d.E = pese2; d.iq = -1;
+                            if (d.E > T.ecut && sp < LSTACK) { lstack[sp++] = p; p = d; }
+                            else push_charged(P, P.eout, P.pout, d, acc, npush, edep_tot, err);
+                            s.state = 0;
+                            continue;
+                        }
+                    } else {
+                        Real pbr1 = rw[11] * s.elke + rw[10];
+                        Real r25 = urand<Real>(p.rng);
+                        if (r25 < pbr1) brems = true;
+                        else {
+                            Real pbr2 = rw[13] * s.elke + rw[12];
+                            if (r25 < pbr2) {   // BHABHA (src/egsnrc.mortran:229-307)
+                                Real peip = p.E, ekin = peip - rm, t0 = ekin / rm, e0 = t0 + 1;
+                                Real yy = 1 / (t0 + 2), e02 = e0 * e0, beta2b = (e02 - 1) / e02;
+                                Real ep0 = M2.te / ekin, ep0c = 1 - ep0, y2 = yy * yy, yp = 1 - 2 * yy, yp2 = yp * yp;
+                                Real b4 = yp2 * yp, b3 = b4 + yp2, b2 = yp * (3 + y2), b1 = 2 - y2, br, rejf2, r04;
+                                int it = 0;
+                                do {
+                                    Real r03 = urand<Real>(p.rng);
+                                    br = ep0 / (1 - ep0c * r03);
+                                    r04 = urand<Real>(p.rng);
+                                    rejf2 = (1 - beta2b * br * (b1 - br * (b2 - br * (b3 - br * b4))));
+                                    if (++it > LOOP_CAP) { err = 1; break; }
+                                } while (!(r04 <= rejf2));
+                                int iq_np = 1, iq_new = -1;
+                                if (!(br < (Real)0.5)) { iq_np = -1; iq_new = 1; br = 1 - br; }
+                                br = dmax(br, (Real)0);
+                                Real pekse2 = br * ekin, pese1 = peip - pekse2, pese2 = pekse2 + rm;
+                                Real h1 = (peip + rm) / ekin;
+                                Real dcosth = dmin((Real)1, h1 * (pese1 - rm) / (pese1 + rm));
+                                Real sinthe = dsqrt(dmax((Real)0, 1 - dcosth)), costhe = dsqrt(dcosth);
+                                Azim<Real> az = azimuth<Real>(p.rng, err);
+                                Real a = p.u, b = p.v, c = p.w;
+                                rotate(a, b, c, sinthe, costhe, az, p.u, p.v, p.w);
+                                p.E = pese1; p.iq = iq_np;
+                                Particle<Real> d = p;
+                                d.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
+                                dcosth = h1 * (pese2 - rm) / (pese2 + rm);
+                                sinthe = -dsqrt(dmax((Real)0, 1 - dcosth));
+                                costhe = dsqrt(dmin((Real)1, dcosth));
+                                rotate(a, b, c, sinthe, costhe, az, d.u, d.v, d.w);
+                                d.E = pese2; d.iq = iq_new;
+                                if (d.E > T.ecut && sp < LSTACK) { lstack[sp++] = p; p = d; }
+                                else push_charged(P, P.eout, P.pout, d, acc, npush, edep_tot, err);
+                                s.state = 0;
+                                continue;
+                            }
+                            // ANNIH in flight (src/egsnrc.mortran:70-182)
+                            Real pavip = p.E + rm, avip = pavip, a = avip / rm, gg = a - 1, tt = gg - 1;
+                            Real pp = dsqrt(a * tt), pot = pp / tt, ep0 = 1 / (a + pp), wsamp = dlog((1 - ep0) / ep0);
+                            Real aa = p.u, bb = p.v, cc = p.w, ep, r02, rejf;
+                            int it = 0;
+                            do {
+                                Real r01 = urand<Real>(p.rng);
+                                ep = ep0 * dexp(r01 * wsamp);
+                                r02 = urand<Real>(p.rng);
+                                rejf = 1 - (ep * a - 1) * (ep * a - 1) / (ep * (a * a - 2));
+                                if (++it > LOOP_CAP) { err = 1; break; }
+                            } while (!(r02 <= rejf));
+                            Real esg1 = avip * ep;
+                            Real costhe = dmax((Real)-1, dmin((Real)1, (esg1 - rm) * pot / esg1));
+                            Real sinthe = dsqrt(1 - costhe * costhe);
+                            Azim<Real> az = azimuth<Real>(p.rng, err);
+                            Particle<Real> g1 = p, g2 = p;
+                            g1.E = esg1; g1.iq = 0;
+                            rotate(aa, bb, cc, sinthe, costhe, az, g1.u, g1.v, g1.w);
+                            g2.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
+                            Real esg2 = pavip - esg1;
+                            g2.E = esg2; g2.iq = 0;
+                            costhe = dmax((Real)-1, dmin((Real)1, (esg2 - rm) * pot / esg2));
+                            sinthe = -dsqrt(1 - costhe * costhe);
+                            rotate(aa, bb, cc, sinthe, costhe, az, g2.u, g2.v, g2.w);
+                            q_push(P, P.pout, g1, npush);
+                            q_push(P, P.pout, g2, npush);
+                            alive = false;
+                            continue;
+                        }
+                    }
+                    // BREMS, BH cross section with KM angles (src/egsnrc.mortran:312-524)
+                    {
+                        Real peie = p.E, ekin = peie - rm, brmin = M2.ap / ekin, waux = s.elke - M2.log_ap;
+                        int l = (peie < 50) ? 0 : 2, l1 = l + 1;
+                        Real a = p.u, b = p.v, c = p.w, sinpsi = a * a + b * b, sindel = 0, cosdel = 0;
+                        if (sinpsi > (Real)1e-20) { sinpsi = dsqrt(sinpsi); sindel = b / sinpsi; cosdel = a / sinpsi; }
+                        Real tteie = peie / rm;
+                        Real beta = dsqrt((tteie - 1) * (tteie + 1)) / tteie;
+                        Real y2max = 2 * beta * (1 + beta) * tteie * tteie, y2maxi = 1 / y2max;
+                        Real z2maxi = dsqrt(y2max + 1);
+                        Real esg, ese, r07, rejf;
+                        int it = 0;
+                        do {
+                            Real r06 = urand<Real>(p.rng);
+                            r07 = urand<Real>(p.rng);
+                            Real br = brmin * dexp(r06 * waux);
+                            esg = ekin * br;
+                            ese = peie - esg;
+                            Real delta = esg / peie / ese * M2.delcm, aux = ese / peie, phi1, phi2;
+                            if (delta < 1) {
+                                phi1 = M2.dl[0][l] + delta * (M2.dl[1][l] + delta * M2.dl[2][l]);
+                                phi2 = M2.dl[0][l1] + delta * (M2.dl[1][l1] + delta * M2.dl[2][l1]);
+                            } else {
+                                phi1 = M2.dl[3][l] + M2.dl[4][l] * dlog(delta + M2.dl[5][l]);
+                                phi2 = phi1;
+                            }
+                            rejf = (1 + aux * aux) * phi1 - 2 * aux * phi2 / 3;
+                            if (++it > LOOP_CAP) { err = 1; break; }
+                        } while (!(r07 < rejf));
+                        Real ttese = ese / rm, esedei = ttese / tteie, rjarg1 = 1 + esedei * esedei;
+                        Real rjarg2 = rjarg1 + 2 * esedei;
+                        Real aux = 2 * ese * tteie / esg;
+                        aux = aux * aux;
+                        Real aux1 = aux * M2.zbrang, rjarg3;
+                        if (aux1 > 10) rjarg3 = M2.lzbrang + (1 - aux1) / (aux1 * aux1);
+                        else rjarg3 = dlog(aux / (1 + aux1));
+                        Real rejmax = rjarg1 * rjarg3 - rjarg2, y2tst, rtest;
+                        it = 0;
+                        while (true) {
+                            y2tst = urand<Real>(p.rng);
+                            rtest = urand<Real>(p.rng);
+                            Real aux3 = z2maxi / (y2tst + (1 - y2tst) * z2maxi);
+                            rtest = rtest * aux3 * rejmax;
+                            y2tst = aux3 * aux3 - 1;
+                            Real a34 = aux3 * aux3 * aux3 * aux3;
+                            Real y2tst1 = esedei * y2tst / a34;
+                            Real aux4 = 16 * y2tst1 - rjarg2, aux5 = rjarg1 - 4 * y2tst1;
+                            if (rtest < aux4 + aux5 * rjarg3) break;
+                            Real aux2 = dlog(aux / (1 + aux1 / a34));
+                            Real rejtst = aux4 + aux5 * aux2;
+                            if (rtest < rejtst) break;
+                            if (++it > LOOP_CAP) { err = 1; break; }
+                        }
+                        Real costhe = 1 - 2 * y2tst * y2maxi;
+                        Real sinthe = dsqrt(dmax((1 - costhe) * (1 + costhe), (Real)0));
+                        Azim<Real> az = azimuth<Real>(p.rng, err);
+                        Particle<Real> gph = p;
+                        gph.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
+                        gph.E = esg; gph.iq = 0;
+                        if (sinpsi >= (Real)1e-10) {
+                            Real us = sinthe * az.c, vs = sinthe * az.s;
+                            gph.u = c * cosdel * us - sindel * vs + a * costhe;
+                            gph.v = c * sindel * us + cosdel * vs + b * costhe;
+                            gph.w = c * costhe - sinpsi * us;
+                        } else { gph.u = sinthe * az.c; gph.v = sinthe * az.s; gph.w = c * costhe; }
+                        q_push(P, P.pout, gph, npush);
+                        p.E = ese;
+                        s.state = 0;
+                        continue;
+                    }
+                }
+                continue;
+            }
+        }
+        if (!alive || s.state == 3) continue;
 
         const int qel = (1 + p.iq) / 2;
         bool ecut_discard = false;
@@ -811,196 +1060,8 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                         Real sigf = ef.sig(s.elke) / ef.dedx(s.elke);
                         Real rfict = urand<Real>(p.rng);
                         if (!(rfict <= sigf / s.sig0)) { s.state = 1; continue; }
-                        // discrete interaction
-                        ++ninter;
-                        const Real *rw = ef.r;
-                        bool brems = false;
-                        if (p.iq < 0) {
-                            Real ebr1 = rw[9] * s.elke + rw[8];
-                            Real r24 = urand<Real>(p.rng);
-                            brems = r24 <= ebr1;
-                            if (!brems && p.E <= M2.thmoll) {
-                                if (ebr1 <= 0) { s.state = 0; continue; }
-                                brems = true;
-                            }
-                            if (!brems) {   // MOLLER (src/egsnrc.mortran:2599-2746)
-                                Real peie = p.E, ekin = peie - rm;
-                                if (ekin <= 2 * M2.te) { s.state = 0; continue; }
-                                Real t0 = ekin / rm, e0 = t0 + 1, extrae = peie - M2.thmoll, e02 = e0 * e0;
-                                Real g2 = t0 * t0 / e02, g3 = (2 * t0 + 1) / e02, gmax = 1 + (Real)1.25 * g2, br, rejf4, r28;
-                                int it = 0;
-                                do {
-                                    Real r27 = urand<Real>(p.rng);
-                                    br = M2.te / (ekin - extrae * r27);
-                                    Real rr2 = br / (1 - br);
-                                    r28 = urand<Real>(p.rng);
-                                    rejf4 = 1 + g2 * br * br + rr2 * (rr2 - g3);
-                                    r28 = gmax * r28;
-                                    if (++it > LOOP_CAP) { err = 1; break; }
-                                } while (!(r28 <= rejf4));
-                                Real pekse2 = br * ekin, pese1 = peie - pekse2, pese2 = pekse2 + rm;
-                                Real h1 = (peie + rm) / ekin;
-                                Real dcosth = h1 * (pese1 - rm) / (pese1 + rm);
-                                Real sinthe = dsqrt(dmax((Real)0, 1 - dcosth)), costhe = dsqrt(dmin((Real)1, dcosth));
-                                Azim<Real> az = azimuth<Real>(p.rng, err);
-                                Real a = p.u, b = p.v, c = p.w;
-                                rotate(a, b, c, sinthe, costhe, az, p.u, p.v, p.w);
-                                p.E = pese1;
-                                Particle<Real> d = p;
-                                d.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
-                                dcosth = h1 * (pese2 - rm) / (pese2 + rm);
-                                sinthe = -dsqrt(dmax((Real)0, 1 - dcosth));
-                                costhe = dsqrt(dmin((Real)1, dcosth));
-                                rotate(a, b, c, sinthe, costhe, az, d.u, d.v, d.w);
-                                d.E = pese2; d.iq = -1;
-                                if (d.E > T.ecut && sp < LSTACK) { lstack[sp++] = p; p = d; }
-                                else push_charged(P, P.eout, P.pout, d, acc, npush, edep_tot, err);
-                                s.state = 0;
-                                continue;
-                            }
-                        } else {
-                            Real pbr1 = rw[11] * s.elke + rw[10];
-                            Real r25 = urand<Real>(p.rng);
-                            if (r25 < pbr1) brems = true;
-                            else {
-                                Real pbr2 = rw[13] * s.elke + rw[12];
-                                if (r25 < pbr2) {   // BHABHA (src/egsnrc.mortran:229-307)
-                                    Real peip = p.E, ekin = peip - rm, t0 = ekin / rm, e0 = t0 + 1;
-                                    Real yy = 1 / (t0 + 2), e02 = e0 * e0, beta2b = (e02 - 1) / e02;
-                                    Real ep0 = M2.te / ekin, ep0c = 1 - ep0, y2 = yy * yy, yp = 1 - 2 * yy, yp2 = yp * yp;
-                                    Real b4 = yp2 * yp, b3 = b4 + yp2, b2 = yp * (3 + y2), b1 = 2 - y2, br, rejf2, r04;
-                                    int it = 0;
-                                    do {
-                                        Real r03 = urand<Real>(p.rng);
-                                        br = ep0 / (1 - ep0c * r03);
-                                        r04 = urand<Real>(p.rng);
-                                        rejf2 = (1 - beta2b * br * (b1 - br * (b2 - br * (b3 - br * b4))));
-                                        if (++it > LOOP_CAP) { err = 1; break; }
-                                    } while (!(r04 <= rejf2));
-                                    int iq_np = 1, iq_new = -1;
-                                    if (!(br < (Real)0.5)) { iq_np = -1; iq_new = 1; br = 1 - br; }
-                                    br = dmax(br, (Real)0);
-                                    Real pekse2 = br * ekin, pese1 = peip - pekse2, pese2 = pekse2 + rm;
-                                    Real h1 = (peip + rm) / ekin;
-                                    Real dcosth = dmin((Real)1, h1 * (pese1 - rm) / (pese1 + rm));
-                                    Real sinthe = dsqrt(dmax((Real)0, 1 - dcosth)), costhe = dsqrt(dcosth);
-                                    Azim<Real> az = azimuth<Real>(p.rng, err);
-                                    Real a = p.u, b = p.v, c = p.w;
-                                    rotate(a, b, c, sinthe, costhe, az, p.u, p.v, p.w);
-                                    p.E = pese1; p.iq = iq_np;
-                                    Particle<Real> d = p;
-                                    d.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
-                                    dcosth = h1 * (pese2 - rm) / (pese2 + rm);
-                                    sinthe = -dsqrt(dmax((Real)0, 1 - dcosth));
-                                    costhe = dsqrt(dmin((Real)1, dcosth));
-                                    rotate(a, b, c, sinthe, costhe, az, d.u, d.v, d.w);
-                                    d.E = pese2; d.iq = iq_new;
-                                    if (d.E > T.ecut && sp < LSTACK) { lstack[sp++] = p; p = d; }
-                                    else push_charged(P, P.eout, P.pout, d, acc, npush, edep_tot, err);
-                                    s.state = 0;
-                                    continue;
-                                }
-                                // ANNIH in flight (src/egsnrc.mortran:70-182)
-                                Real pavip = p.E + rm, avip = pavip, a = avip / rm, gg = a - 1, tt = gg - 1;
-                                Real pp = dsqrt(a * tt), pot = pp / tt, ep0 = 1 / (a + pp), wsamp = dlog((1 - ep0) / ep0);
-                                Real aa = p.u, bb = p.v, cc = p.w, ep, r02, rejf;
-                                int it = 0;
-                                do {
-                                    Real r01 = urand<Real>(p.rng);
-                                    ep = ep0 * dexp(r01 * wsamp);
-                                    r02 = urand<Real>(p.rng);
-                                    rejf = 1 - (ep * a - 1) * (ep * a - 1) / (ep * (a * a - 2));
-                                    if (++it > LOOP_CAP) { err = 1; break; }
-                                } while (!(r02 <= rejf));
-                                Real esg1 = avip * ep;
-                                Real costhe = dmax((Real)-1, dmin((Real)1, (esg1 - rm) * pot / esg1));
-                                Real sinthe = dsqrt(1 - costhe * costhe);
-                                Azim<Real> az = azimuth<Real>(p.rng, err);
-                                Particle<Real> g1 = p, g2 = p;
-                                g1.E = esg1; g1.iq = 0;
-                                rotate(aa, bb, cc, sinthe, costhe, az, g1.u, g1.v, g1.w);
-                                g2.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
-                                Real esg2 = pavip - esg1;
-                                g2.E = esg2; g2.iq = 0;
-                                costhe = dmax((Real)-1, dmin((Real)1, (esg2 - rm) * pot / esg2));
-                                sinthe = -dsqrt(1 - costhe * costhe);
-                                rotate(aa, bb, cc, sinthe, costhe, az, g2.u, g2.v, g2.w);
-                                q_push(P, P.pout, g1, npush);
-                                q_push(P, P.pout, g2, npush);
-                                alive = false;
-                                continue;
-                            }
-                        }
-                        // BREMS, BH cross section with KM angles (src/egsnrc.mortran:312-524)
-                        {
-                            Real peie = p.E, ekin = peie - rm, brmin = M2.ap / ekin, waux = s.elke - M2.log_ap;
-                            int l = (peie < 50) ? 0 : 2, l1 = l + 1;
-                            Real a = p.u, b = p.v, c = p.w, sinpsi = a * a + b * b, sindel = 0, cosdel = 0;
-                            if (sinpsi > (Real)1e-20) { sinpsi = dsqrt(sinpsi); sindel = b / sinpsi; cosdel = a / sinpsi; }
-                            Real tteie = peie / rm;
-                            Real beta = dsqrt((tteie - 1) * (tteie + 1)) / tteie;
-                            Real y2max = 2 * beta * (1 + beta) * tteie * tteie, y2maxi = 1 / y2max;
-                            Real z2maxi = dsqrt(y2max + 1);
-                            Real esg, ese, r07, rejf;
-                            int it = 0;
-                            do {
-                                Real r06 = urand<Real>(p.rng);
-                                r07 = urand<Real>(p.rng);
-                                Real br = brmin * dexp(r06 * waux);
-                                esg = ekin * br;
-                                ese = peie - esg;
-                                Real delta = esg / peie / ese * M2.delcm, aux = ese / peie, phi1, phi2;
-                                if (delta < 1) {
-                                    phi1 = M2.dl[0][l] + delta * (M2.dl[1][l] + delta * M2.dl[2][l]);
-                                    phi2 = M2.dl[0][l1] + delta * (M2.dl[1][l1] + delta * M2.dl[2][l1]);
-                                } else {
-                                    phi1 = M2.dl[3][l] + M2.dl[4][l] * dlog(delta + M2.dl[5][l]);
-                                    phi2 = phi1;
-                                }
-                                rejf = (1 + aux * aux) * phi1 - 2 * aux * phi2 / 3;
-                                if (++it > LOOP_CAP) { err = 1; break; }
-                            } while (!(r07 < rejf));
-                            Real ttese = ese / rm, esedei = ttese / tteie, rjarg1 = 1 + esedei * esedei;
-                            Real rjarg2 = rjarg1 + 2 * esedei;
-                            Real aux = 2 * ese * tteie / esg;
-                            aux = aux * aux;
-                            Real aux1 = aux * M2.zbrang, rjarg3;
-                            if (aux1 > 10) rjarg3 = M2.lzbrang + (1 - aux1) / (aux1 * aux1);
-                            else rjarg3 = dlog(aux / (1 + aux1));
-                            Real rejmax = rjarg1 * rjarg3 - rjarg2, y2tst, rtest;
-                            it = 0;
-                            while (true) {
-                                y2tst = urand<Real>(p.rng);
-                                rtest = urand<Real>(p.rng);
-                                Real aux3 = z2maxi / (y2tst + (1 - y2tst) * z2maxi);
-                                rtest = rtest * aux3 * rejmax;
-                                y2tst = aux3 * aux3 - 1;
-                                Real a34 = aux3 * aux3 * aux3 * aux3;
-                                Real y2tst1 = esedei * y2tst / a34;
-                                Real aux4 = 16 * y2tst1 - rjarg2, aux5 = rjarg1 - 4 * y2tst1;
-                                if (rtest < aux4 + aux5 * rjarg3) break;
-                                Real aux2 = dlog(aux / (1 + aux1 / a34));
-                                Real rejtst = aux4 + aux5 * aux2;
-                                if (rtest < rejtst) break;
-                                if (++it > LOOP_CAP) { err = 1; break; }
-                            }
-                            Real costhe = 1 - 2 * y2tst * y2maxi;
-                            Real sinthe = dsqrt(dmax((1 - costhe) * (1 + costhe), (Real)0));
-                            Azim<Real> az = azimuth<Real>(p.rng, err);
-                            Particle<Real> gph = p;
-                            gph.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
-                            gph.E = esg; gph.iq = 0;
-                            if (sinpsi >= (Real)1e-10) {
-                                Real us = sinthe * az.c, vs = sinthe * az.s;
-                                gph.u = c * cosdel * us - sindel * vs + a * costhe;
-                                gph.v = c * sindel * us + cosdel * vs + b * costhe;
-                                gph.w = c * costhe - sinpsi * us;
-                            } else { gph.u = sinthe * az.c; gph.v = sinthe * az.s; gph.w = c * costhe; }
-                            q_push(P, P.pout, gph, npush);
-                            p.E = ese;
-                            s.state = 0;
-                            continue;
-                        }
+                        s.state = 3;   // interaction due: wait for the warp's batch
+                        continue;
                     }
                 }
             }
@@ -1413,6 +1474,7 @@ struct Engine : EngineBase {
         P.peak = (unsigned *)d_counts.p + 8;
         P.seed = seed;
         P.requeue_lanes = cfg.requeue_lanes > 0 ? cfg.requeue_lanes : 0;
+        P.inter_batch = cfg.inter_batch > 0 ? std::min(cfg.inter_batch, 32) : (cfg.inter_batch < 0 ? 1 : 8);
         P.pin = q[0]; P.ein = q[2]; P.pout = q[0]; P.eout = q[2];
         const bool use_graph = cfg.use_graph > 0 && graph_ok;
         if (use_graph) build_graph(P, grid, bs);

@@ -51,6 +51,9 @@ typedef struct {
                              (default; results are identical either way) */
     int use_graph;        /* 1: replay the wavefront rounds from a CUDA graph (no
                              per-kernel timing); 0: direct launches with CUDA events */
+    int inter_batch;      /* lanes of a warp due to interact before their interactions
+                             are sampled together; 0 = default (8), -1 = immediately
+                             (results are identical either way) */
 } egsgpu_config;
 
 /* Source: egs++ EGS_ParallelBeam (sources/egs_parallel_beam) with a point

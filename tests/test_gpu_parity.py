@@ -208,13 +208,16 @@ def test_chunking_invariance(precision):
 
 
 @pytest.mark.parametrize("precision", [32, 64])
-def test_requeue_invariance(precision):
-    # parking sparse warps' particles in the next round changes scheduling only
-    wl = W.water128e(32)
+@pytest.mark.parametrize("workload", ["water128e", "slab64"])
+def test_scheduling_invariance(precision, workload):
+    # parking sparse warps' particles in the next round and batching the
+    # interactions of a warp change the scheduling only
+    wl = W.WORKLOADS[workload](32)
     n = 40000
     res = []
-    for lanes in (-1, 16):
-        eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"], precision=precision, requeue_lanes=lanes)
+    for lanes, inter in ((-1, -1), (16, 8), (-1, 24)):
+        eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"], precision=precision, requeue_lanes=lanes,
+                            inter_batch=inter)
         eng.set_geometry(wl["geometry"])
         eng.set_source(wl["source"])
         eng.set_history_tally(0, n)
@@ -223,7 +226,8 @@ def test_requeue_invariance(precision):
     # FP32: a parked particle's pending per-voxel FP32 partial sum is split in
     # two, which regroups float additions (relative 1e-7 per deposit)
     tol = 1e-12 if precision == 64 else 2e-5
-    assert np.allclose(res[0], res[1], rtol=tol, atol=tol)
+    for r in res[1:]:
+        assert np.allclose(res[0], r, rtol=tol, atol=tol)
 
 
 def test_graph_replay_matches_direct_launches():

@@ -1474,7 +1474,7 @@ struct Engine : EngineBase {
         P.peak = (unsigned *)d_counts.p + 8;
         P.seed = seed;
         P.requeue_lanes = cfg.requeue_lanes > 0 ? cfg.requeue_lanes : 0;
-        P.inter_batch = cfg.inter_batch > 0 ? std::min(cfg.inter_batch, 32) : (cfg.inter_batch < 0 ? 1 : 8);
+        P.inter_batch = cfg.inter_batch > 0 ? std::min(cfg.inter_batch, 32) : (cfg.inter_batch < 0 ? 1 : 12);
         P.pin = q[0]; P.ein = q[2]; P.pout = q[0]; P.eout = q[2];
         const bool use_graph = cfg.use_graph > 0 && graph_ok;
         if (use_graph) build_graph(P, grid, bs);

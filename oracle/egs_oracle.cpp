@@ -22,6 +22,13 @@
 // The tables come from the host data layer (egsnrc_gb300/csrc/egs_hatch.cpp),
 // whose values are pinned separately against the raw data files.
 //
+// Pinning: the RANMAR generator is pinned to the one golden vector the
+// reference ships for this path (user_codes/ranmar_test).  Transport physics
+// parity is UNPINNED: the reference has no transport, dose or cross-section
+// golden values, and its transport core (Mortran3 -> Fortran 77) cannot be
+// compiled without a Fortran compiler, so no reference run checks this
+// restatement.
+//
 // Random numbers: either one RANMAR stream for the whole run (as the
 // reference does) or Philox-4x32-10 (Salmon et al., SC'11) with one stream
 // per particle keyed by (seed, history) and a 64-bit stream id; children get

@@ -43,6 +43,7 @@ class SourceStruct(C.Structure):
 
 
 _LIB = None
+NOALLOC_MAX_HISTORIES = 2048   # EGSGPU_NOALLOC_MAX_HISTORIES in include/egsgpu.h
 
 
 def library_path():
@@ -65,6 +66,7 @@ def load_library():
     L.egsgpu_set_xyz_geometry.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp, dp, dp, C.POINTER(C.c_int32), dp]
     L.egsgpu_set_source.argtypes = [vp, C.POINTER(SourceStruct)]
     L.egsgpu_run.argtypes = [vp, i64, i64, C.c_int, C.c_uint32, vp]
+    L.egsgpu_run_noalloc.argtypes = [vp, i64, i64, C.c_uint32, vp, vp]
     L.egsgpu_reset.argtypes = [vp]
     L.egsgpu_get_tallies.argtypes = [vp, dp, dp, dp]
     L.egsgpu_get_dose.argtypes = [vp, dp, dp]
@@ -188,6 +190,15 @@ class DoseEngine:
     def run(self, n, nbatch=10, seed=1, first=0, stream=None):
         st = C.c_void_p(stream) if stream else None
         self._check(self.L.egsgpu_run(self.h, int(first), int(n), int(nbatch), int(seed), st))
+
+    def run_noalloc(self, dose_ptr, n, seed=1, first=0, stream=None):
+        """Transports histories [first, first+n) into the caller's device
+        array of nvox doubles at address `dose_ptr` (overwritten with this
+        call's energy per voxel, MeV) without allocating device memory; the
+        handle's own tallies are untouched.  At most NOALLOC_MAX_HISTORIES
+        histories per call; calls overlapping on the GPU race."""
+        st = C.c_void_p(stream) if stream else None
+        self._check(self.L.egsgpu_run_noalloc(self.h, int(first), int(n), int(seed), C.c_void_p(dose_ptr), st))
 
     def reset(self):
         self._check(self.L.egsgpu_reset(self.h))

@@ -26,6 +26,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1144,6 +1145,8 @@ struct EngineBase {
                          const int32_t *med, const double *rhor, std::string &err) = 0;
     virtual int run(const Source &S, long long first, long long n, int nbatch, uint32_t seed, cudaStream_t st,
                     std::string &err) = 0;
+    virtual int run_noalloc(const Source &S, long long first, long long n, uint32_t seed, double *dose,
+                            cudaStream_t st, unsigned char *scratch, size_t scratch_bytes, std::string &err) = 0;
 };
 
 template <class Real>
@@ -1551,6 +1554,85 @@ struct Engine : EngineBase {
         if (e[1]) { err = "a device sampling loop hit its iteration cap"; return EGSGPU_ERR_LOOP; }
         return 0;
     }
+
+    // Transport of one small chunk with every piece of scratch (queues,
+    // counters, error flags) carved out of a caller-independent static device
+    // array; all work goes to the caller's stream.  See egsgpu_run_noalloc.
+    int run_noalloc(const Source &S, long long first, long long n, uint32_t seed, double *dose, cudaStream_t st,
+                    unsigned char *scratch, size_t scratch_bytes, std::string &err) override {
+        if (!G.xb) { err = "geometry not set"; return EGSGPU_ERR_STATE; }
+        // layout: 1 KiB of counters, then four queues of equal capacity
+        unsigned *counts = (unsigned *)scratch;                          // 16 x unsigned
+        double *energy = (double *)(scratch + 256);                      // 2 x double
+        unsigned long long *counters = (unsigned long long *)(scratch + 512);   // CNT_N
+        int *error = (int *)(scratch + 896);                             // 2 x int
+        const size_t rec = 12 * sizeof(Real) + sizeof(int) + 2 + 2 * sizeof(uint32_t) + sizeof(unsigned long long);
+        size_t avail = scratch_bytes - 1024 - 4 * 16 * 256;
+        unsigned cap = (unsigned)((avail / (4 * rec)) & ~(size_t)255);
+        Queue<Real> Q[4];
+        unsigned char *b = scratch + 1024;
+        auto take = [&](size_t bytes) { unsigned char *r = b; b += (bytes + 255) & ~(size_t)255; return r; };
+        for (int k = 0; k < 4; ++k) {
+            Queue<Real> &q = Q[k];
+            q.x = (Real *)take(cap * sizeof(Real)); q.y = (Real *)take(cap * sizeof(Real));
+            q.z = (Real *)take(cap * sizeof(Real)); q.u = (Real *)take(cap * sizeof(Real));
+            q.v = (Real *)take(cap * sizeof(Real)); q.w = (Real *)take(cap * sizeof(Real));
+            q.E = (Real *)take(cap * sizeof(Real)); q.wt = (Real *)take(cap * sizeof(Real));
+            q.ir = (int *)take(cap * sizeof(int)); q.iq = (int8_t *)take(cap);
+            q.hist = (uint32_t *)take(cap * sizeof(uint32_t)); q.n = (uint32_t *)take(cap * sizeof(uint32_t));
+            q.sid = (unsigned long long *)take(cap * sizeof(unsigned long long));
+            q.st = (uint8_t *)take(cap);
+            q.aux0 = (Real *)take(cap * sizeof(Real)); q.aux1 = (Real *)take(cap * sizeof(Real));
+            q.aux2 = (Real *)take(cap * sizeof(Real)); q.aux3 = (Real *)take(cap * sizeof(Real));
+            q.count = counts + 2 * k;
+            q.capacity = cap;
+        }
+        if ((size_t)(b - scratch) > scratch_bytes) { err = "no-allocation scratch layout overflow"; return EGSGPU_ERR_STATE; }
+        const int bs = 128;
+        int occ_p = 1, occ_e = 1;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real>, bs, 0));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real>, bs, 0));
+        const int grid = sm_count * std::max(1, std::min(occ_p, occ_e));
+        Params<Real> P;
+        P.T = T; P.G = G;
+        P.dose = dose;
+        P.hist_tally = nullptr; P.hist_first = 0; P.hist_n = 0;
+        P.energy = energy; P.counters = counters; P.error = error; P.peak = counts + 8;
+        P.seed = seed;
+        P.requeue_lanes = 0;
+        P.inter_batch = 12;
+        // the array keeps the previous call's contents: clear the counters
+        CK(cudaMemsetAsync(scratch, 0, 1024, st));
+        CK(cudaMemsetAsync(dose, 0, (size_t)nvox * sizeof(double), st));
+        P.pout = Q[0]; P.eout = Q[2]; P.pin = Q[0]; P.ein = Q[2];
+        k_source<Real><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(P, S, first, n);
+        CK(cudaGetLastError());
+        int cur = 0;
+        bool done = false;
+        for (int round = 0; round < 100000 && !done; ++round) {
+            int nxt = 1 - cur;
+            CK(cudaMemsetAsync(counts + 2 * nxt, 0, 2 * sizeof(unsigned), st));
+            CK(cudaMemsetAsync(counts + 4 + 2 * nxt, 0, 2 * sizeof(unsigned), st));
+            P.pin = Q[cur]; P.ein = Q[2 + cur]; P.pout = Q[nxt]; P.eout = Q[2 + nxt];
+            k_photon<Real><<<grid, bs, 0, st>>>(P);
+            CK(cudaGetLastError());
+            k_electron<Real><<<grid, bs, 0, st>>>(P);
+            CK(cudaGetLastError());
+            unsigned h[9];
+            CK(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            if (h[8] > cap) { err = "no-allocation scratch queues overflowed; transport fewer histories per call"; return EGSGPU_ERR_CAPACITY; }
+            cur = nxt;
+            done = h[2 * cur] == 0 && h[4 + 2 * cur] == 0;
+        }
+        if (!done) { err = "wavefront did not drain"; return EGSGPU_ERR_LOOP; }
+        int e[2];
+        CK(cudaMemcpyAsync(e, error, sizeof(e), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (e[0]) { err = "no-allocation scratch queues overflowed"; return EGSGPU_ERR_CAPACITY; }
+        if (e[1]) { err = "a device sampling loop hit its iteration cap"; return EGSGPU_ERR_LOOP; }
+        return 0;
+    }
 };
 
 }  // namespace
@@ -1881,6 +1963,53 @@ int egsgpu_restore(egsgpu_handle *h, const void *buf, size_t size) {
     h->nhist = hdr[2];
     h->nbatch = (int)hdr[3];
     return 0;
+}
+
+}  // extern "C"
+
+// Scratch of egsgpu_run_noalloc, the entry point for callers that may not
+// allocate device memory while they transport: code recording a CUDA stream
+// capture (an allocation there is an error or leaves the graph owning the
+// memory), a time-critical loop that must not wait on the allocator, or a host
+// framework whose memory pool owns every allocation on the device.  The array
+// is a fixed part of the module: it exists on every GPU the library is used
+// on and costs EGSGPU_NOALLOC_SCRATCH_MIB of device memory there until the
+// process exits.  Host code cannot use the name as an address; the device
+// address is looked up once per device with cudaGetSymbolAddress.  All calls
+// share the one array, and each call clears the counters it relies on.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[(size_t)EGSGPU_NOALLOC_SCRATCH_MIB << 20];
+static std::mutex g_noalloc_mutex;
+static unsigned char *g_noalloc_addr[256] = {};
+
+extern "C" {
+
+int egsgpu_run_noalloc(egsgpu_handle *h, long long first, long long n, uint32_t seed, double *dose, void *stream) {
+    if (!h || !dose || n < 0 || first < 0 || first + n > 0xffffffffLL) return EGSGPU_ERR_ARG;
+    if (n > EGSGPU_NOALLOC_MAX_HISTORIES) {
+        h->err = "egsgpu_run_noalloc: at most " + std::to_string(EGSGPU_NOALLOC_MAX_HISTORIES) +
+                 " histories per call (the fixed scratch holds the particle queues of one chunk)";
+        return EGSGPU_ERR_ARG;
+    }
+    if (!h->have_media || !h->have_geom || !h->have_source) { h->err = "media, geometry and source must be set"; return EGSGPU_ERR_STATE; }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) { h->err = "no current CUDA device"; return EGSGPU_ERR_CUDA; }
+    unsigned char *scratch = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (!g_noalloc_addr[dev]) {   // first call on this device: look the array up
+            void *p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p) {
+                h->err = std::string("cudaGetSymbolAddress(no-allocation scratch): ") + cudaGetErrorString(e);
+                return EGSGPU_ERR_CUDA;
+            }
+            g_noalloc_addr[dev] = (unsigned char *)p;
+        }
+        scratch = g_noalloc_addr[dev];
+    }
+    if (n == 0) return 0;
+    return h->eng->run_noalloc(h->S, first, n, seed, dose, (cudaStream_t)stream, scratch,
+                               (size_t)EGSGPU_NOALLOC_SCRATCH_MIB << 20, h->err);
 }
 
 const char *egsgpu_last_error(egsgpu_handle *h) { return h ? h->err.c_str() : "null handle"; }

@@ -153,6 +153,34 @@ int egsgpu_get_profile(egsgpu_handle *h, double *out);
 int egsgpu_checkpoint(egsgpu_handle *h, void *buf, size_t *size);
 int egsgpu_restore(egsgpu_handle *h, const void *buf, size_t size);
 
+/* No-allocation transport, for callers that may not allocate device memory
+ * while they run: code inside a CUDA stream capture, a real-time loop that
+ * must not block on the allocator, or a host framework that owns every
+ * allocation (its memory pool) and forbids others.  This entry point has no
+ * counterpart in the reference API.
+ *
+ * Transports histories [first, first+n) exactly as egsgpu_run would (same
+ * random-number streams, same physics) and writes this call's deposited
+ * energy per voxel (MeV, FP64) into `dose`, a caller-owned device array of
+ * nx*ny*nz doubles on the current device, overwriting it.  The handle's
+ * tallies are not touched.  The particle queues live in a fixed file-scope
+ * device array of EGSGPU_NOALLOC_SCRATCH_MIB MiB that every GPU loading the
+ * library holds until the process exits; the call makes no cudaMalloc or
+ * cudaFree and creates no stream or event.  At most
+ * EGSGPU_NOALLOC_MAX_HISTORIES histories per call (larger n is rejected with
+ * EGSGPU_ERR_ARG); a chunk whose secondaries overflow the queues returns
+ * EGSGPU_ERR_CAPACITY.  All work is ordered on `stream` (NULL = default
+ * stream) and the call returns after it completes.  The first call on each
+ * device looks up the array's device address with cudaGetSymbolAddress;
+ * make that first call before any stream capture.  Every call shares the
+ * one array: calls that overlap on the GPU (from several threads, streams
+ * or handles) race and must be serialised by the caller.  The handle's
+ * media, geometry and source must have been set (those calls allocate). */
+#define EGSGPU_NOALLOC_SCRATCH_MIB 40
+#define EGSGPU_NOALLOC_MAX_HISTORIES 2048
+int egsgpu_run_noalloc(egsgpu_handle *h, long long first, long long n, uint32_t seed, double *dose,
+                       void *stream);
+
 /* Last error message of the handle (never NULL). */
 const char *egsgpu_last_error(egsgpu_handle *h);
 

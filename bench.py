@@ -177,13 +177,16 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+def ncu_traffic(kernel, workload, steps_per_launch):
+    """DRAM bytes (read + write) per launch of `kernel`, from the committed ncu
+    capture of a smaller case of the same workload (profiles/ncu_traffic.json:
+    measured DRAM bytes per transport step), scaled to this run's transport
+    steps per launch; None without a capture of this kernel and workload."""
     p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     try:
         with open(p) as f:
             d = json.load(f)
-        return d.get(kernel)
+        return d[workload][kernel]["dram_bytes_per_step"] * steps_per_launch
     except Exception:
         return None
 
@@ -327,11 +330,14 @@ def main():
     bytes_k = steps_k * ALG_BYTES_PER_STEP + pushes_k * ALG_BYTES_PER_PUSH
     achieved = bytes_k / (ms_k / 1e3) / 1e9 if ms_k > 0 else None
     peak, peak_kind = measured_peak_hbm()
-    traffic = ncu_traffic("k_" + kern)
+    traffic = ncu_traffic("k_" + kern, wl["name"], steps_k / n_k)
     roof = {"bound": "hbm", "kernel": "k_" + kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
             "traffic": traffic, "alg_bytes_per_launch": bytes_k / n_k, "launches": n_k,
             "ms_per_launch": ms_k / n_k, "steps_per_s": steps_k / (ms_k / 1e3) if ms_k > 0 else None,
+            "steps_per_launch": steps_k / n_k, "pushes_per_launch": pushes_k / n_k,
+            "launches_photon": prof["launches_photon"], "launches_electron": prof["launches_electron"],
+            "steps_photon": prof["photon_steps"], "steps_electron": prof["electron_steps"],
             "kernel_share": {k: prof["ms_" + k] / max(1e-9, sum(prof["ms_" + j] for j in
                                                                   ("source", "photon", "electron", "batch")))
                              for k in ("source", "photon", "electron", "batch")}}

@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--chunk", type=int, default=0, help="histories per wavefront chunk (0 = automatic)")
     ap.add_argument("--clock-period", type=float, default=0.2, help="seconds between clock samples")
     ap.add_argument("--clock-mode", default="nvml", choices=["nvml", "process", "off"])
+    ap.add_argument("--scale", type=float, default=0.005,
+                    help="batched64: fraction of each phantom's 1e6-5e7 histories run per step")
     return ap.parse_args()
 
 
@@ -268,11 +270,210 @@ def config_of(wl, per_step):
             "l2": "256 MiB buffer written between timed steps"}
 
 
+def batched_sigma(eng, probs, nb):
+    """Mean squared relative 1-sigma over the voxels above half of each
+    phantom's own maximum, over all phantoms (nb batches)."""
+    s_all, s2_all, _ = eng.tallies()
+    rel2, n = [], 0
+    for k in range(len(probs)):
+        off, nv, _ = eng.phantom_info(k)
+        s, s2 = s_all[off:off + nv], s2_all[off:off + nv]
+        if s.max() <= 0:
+            continue
+        m = s / nb
+        var = np.maximum(s2 / nb - m * m, 0) / max(nb - 1, 1)
+        sel = s > 0.5 * s.max()
+        rel2.append(var[sel] * nb * nb / (s[sel] * s[sel]))
+        n += int(sel.sum())
+    r = np.concatenate(rel2)
+    return float(np.sqrt(np.mean(r))), n
+
+
+def batched_oracle(wl, frac, threads, first):
+    """CPU oracle over every phantom of the batched workload, `frac` of each
+    phantom's step histories; returns (histories, seconds)."""
+    from oracle.oracle_binding import Oracle
+    ora = Oracle(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"])
+    n, t = 0, 0.0
+    for p in wl["problems"]:
+        m = max(threads, int(p["histories"] * frac))
+        ora.set_geometry(p["geometry"])
+        ora.set_source(p["source"])
+        t0 = time.perf_counter()
+        ora.run(m, nbatch=1, seed=p["seed"], first=first, threads=threads)
+        t += time.perf_counter() - t0
+        n += m
+    return n, t
+
+
+def batched_config(wl, args):
+    ps = wl["problems"]
+    return {"workload": "batched64", "phantoms": len(ps), "edges_voxels": [int(p["edge"]) for p in ps][:64],
+            "voxel_cm": 0.2, "media": wl["media"], "histories_per_step": int(sum(p["histories"] for p in ps)),
+            "history_scale": args.scale, "batches_per_step": 1, "ecut_MeV": wl["ecut"], "pcut_MeV": wl["pcut"],
+            "l2": "256 MiB buffer written between timed steps"}
+
+
+def bench_batched(args, ws, rank, local, dist):
+    """Many phantoms per step (one egsgpu_run_phantoms call) against the same
+    phantoms run one after another."""
+    from egsnrc_gb300 import workloads as W
+    wl = W.batched64(scale=args.scale)
+    ps = wl["problems"]
+    for p in ps:          # every rank transports its own histories (weak scaling)
+        p["seed"] += 7919 * rank
+    H = sum(p["histories"] for p in ps)
+    K, Wm = args.steps, args.warmup
+    threads = os.cpu_count() or 1
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        n0, t0 = batched_oracle(wl, 2e-3, threads, 0)
+        frac = 2e-3 * 4.0 / max(t0, 1e-3)          # about 4 s of host work per step
+        for _ in range(Wm):
+            batched_oracle(wl, frac, threads, 10 ** 7)
+        n, T = 0, 0.0
+        for _ in range(K):
+            a, b = batched_oracle(wl, frac, threads, 2 * 10 ** 7)
+            n += a; T += b
+        value = n / T
+        line = {"impl": "reference", "metric": "histories_per_second", "value": value, "unit": "histories/s",
+                "n_gpus": args.gpus, "steps": K, "warmup": Wm, "ms_per_step": 1e3 * T / K,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": batched_config(wl, args),
+                "cpu_baseline": {"value": value, "unit": "histories/s", "cores": threads, "kind": "port",
+                                 "sample": "%.2g of every phantom's step histories per step x %d steps (FP64 CPU "
+                                           "restatement, one thread per core)" % (frac, K)},
+                "e2e": {"value": value, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    import torch
+    import egsnrc_gb300 as eg
+    torch.cuda.set_device(local)
+    ekw = dict(capacity=args.capacity, chunk=args.chunk)
+    eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], precision=args.precision, **ekw)
+    eng.set_phantoms(ps)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    flush.zero_()
+    torch.cuda.synchronize()
+    for _ in range(Wm):
+        eng.run_phantoms(nbatch=1)
+    eng.reset()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local, args.clock_period, args.clock_mode) as clk:
+        torch.cuda.synchronize()
+        start.record()
+        for _ in range(K):
+            flush.zero_()
+            eng.run_phantoms(nbatch=1)
+        stop.record()
+        torch.cuda.synchronize()
+    T = start.elapsed_time(stop) / 1e3
+    if dist:
+        tt = torch.tensor([T], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        T = float(tt.item())
+    prof = eng.profile()
+    sig, nsel = batched_sigma(eng, ps, K) if K > 1 else (None, 0)
+    value = H * ws * K / T
+    eff = (1.0 / (sig * sig * T)) if sig else None
+    kern = "electron" if prof["ms_electron"] >= prof["ms_photon"] else "photon"
+    steps_k, pushes_k = prof[kern + "_steps"], prof[kern + "_pushes"]
+    ms_k, n_k = prof["ms_" + kern], max(prof["launches_" + kern], 1)
+    bytes_k = steps_k * ALG_BYTES_PER_STEP + pushes_k * ALG_BYTES_PER_PUSH
+    achieved = bytes_k / (ms_k / 1e3) / 1e9 if ms_k > 0 else None
+    peak, peak_kind = measured_peak_hbm()
+    roof = {"bound": "hbm", "kernel": "k_" + kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
+            "traffic": ncu_traffic("k_" + kern, "batched64", steps_k / n_k), "alg_bytes_per_launch": bytes_k / n_k,
+            "launches": n_k, "ms_per_launch": ms_k / n_k, "steps_per_launch": steps_k / n_k,
+            "kernel_share": {k: prof["ms_" + k] / max(1e-9, sum(prof["ms_" + j] for j in
+                                                                  ("source", "photon", "electron", "batch")))
+                             for k in ("source", "photon", "electron", "batch")}}
+    launches = sum(prof["launches_" + k] for k in ("source", "photon", "electron", "batch"))
+    eng.close()
+
+    # e2e: phantoms uploaded from host arrays, run, tallies read back, every step
+    e2e_eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], precision=args.precision, **ekw)
+    h2d = sum(p["geometry"].xb.nbytes + p["geometry"].yb.nbytes + p["geometry"].zb.nbytes + p["geometry"].med.nbytes
+              + p["geometry"].rhor.nbytes for p in ps)
+    nv_all = sum(p["geometry"].nvox for p in ps)
+    torch.cuda.synchronize()
+    te0 = time.perf_counter()
+    for _ in range(K):
+        flush.zero_()
+        e2e_eng.set_phantoms(ps)
+        e2e_eng.run_phantoms(nbatch=1)
+        e2e_eng.tallies()
+    torch.cuda.synchronize()
+    Te = time.perf_counter() - te0
+    e2e_eng.close()
+    line = {"metric": "histories_per_second", "value": value, "unit": "histories/s", "n_gpus": ws, "steps": K,
+            "warmup": Wm, "ms_per_step": 1e3 * T / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if args.precision == 32 else "f64", "data": "synthetic",
+            "config": batched_config(wl, args), "dose_efficiency": eff, "dose_efficiency_unit": "1/(sigma^2 s)",
+            "sigma_bar_50pct": sig, "voxels_above_50pct": nsel,
+            "e2e": {"value": H * ws * K / Te, "unit": "histories/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(2 * nv_all * 8 + 64),
+                    "path": "egsgpu_set_phantoms + egsgpu_run_phantoms + egsgpu_get_tallies"},
+            "roofline": roof, "gpu_launches": int(launches)}
+    if rank == 0 and not args.no_fp64:
+        # the same phantoms one after another (egsgpu_run per phantom): FP32, and the plain FP64 form
+        for prec, key, frac in ((args.precision, "one_at_a_time", 1.0), (64, "fp64_one_at_a_time", 0.25)):
+            e1 = eg.DoseEngine(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], precision=prec, **ekw)
+            n1, T1 = 0, 0.0
+            rel2 = []
+            for p in ps:
+                e1.set_geometry(p["geometry"])
+                e1.set_source(p["source"])
+                m = max(2, int(p["histories"] * frac))
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                for k in range(2):
+                    e1.run(m, nbatch=1, seed=p["seed"], first=k * m)
+                torch.cuda.synchronize()
+                T1 += time.perf_counter() - t0
+                n1 += 2 * m
+                s1, s21, _ = e1.tallies()
+                if s1.max() > 0:
+                    mm = s1 / 2
+                    var = np.maximum(s21 / 2 - mm * mm, 0)
+                    sel = s1 > 0.5 * s1.max()
+                    rel2.append(var[sel] * 4 / (s1[sel] * s1[sel]))
+            e1.close()
+            sig1 = float(np.sqrt(np.mean(np.concatenate(rel2))))
+            line[key] = {"value": n1 / T1, "unit": "histories/s", "dose_efficiency": 1.0 / (sig1 * sig1 * T1),
+                         "histories_fraction": frac}
+        if eff:
+            line["efficiency_ratio_batched_fp32_over_fp64"] = eff / line["fp64_one_at_a_time"]["dose_efficiency"]
+    line["clocks"] = clk.summary()
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        n0, t0 = batched_oracle(wl, 1e-3, threads, 10 ** 8)
+        frac = 1e-3 * args.cpu_seconds / max(t0, 1e-3)
+        n, dt = batched_oracle(wl, frac, threads, 2 * 10 ** 8)
+        line["cpu_baseline"] = {"value": n / dt, "unit": "histories/s", "cores": threads, "kind": "port",
+                                "sample": "%d histories over all %d phantoms on %d host threads, %.1f s"
+                                          % (n, len(ps), threads, dt)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
 def main():
     args = parse()
     from egsnrc_gb300 import workloads as W
-    wl = W.WORKLOADS[args.workload]()
     ws, rank, local, dist = dist_setup(args)
+    if args.workload == "batched64":
+        bench_batched(args, ws, rank, local, dist)
+        if dist and args.impl == "reference":
+            dist.barrier()
+        return
+    wl = W.WORKLOADS[args.workload]()
     if args.impl == "reference":
         reference_arm(args, wl, ws, rank, dist)
         if dist:

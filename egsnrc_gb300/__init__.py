@@ -39,7 +39,8 @@ class SourceStruct(C.Structure):
     _fields_ = [("charge", C.c_int), ("shape", C.c_int), ("pos", C.c_double * 3), ("xmin", C.c_double),
                 ("xmax", C.c_double), ("ymin", C.c_double), ("ymax", C.c_double), ("dir", C.c_double * 3),
                 ("spectrum", C.c_int), ("energy", C.c_double), ("nbins", C.c_int),
-                ("edges", C.POINTER(C.c_double)), ("weights", C.POINTER(C.c_double))]
+                ("edges", C.POINTER(C.c_double)), ("weights", C.POINTER(C.c_double)),
+                ("nphsp", C.c_longlong), ("phsp", C.POINTER(C.c_float)), ("recycle", C.c_int)]
 
 
 _LIB = None
@@ -68,6 +69,11 @@ def load_library():
     L.egsgpu_run.argtypes = [vp, i64, i64, C.c_int, C.c_uint32, vp]
     L.egsgpu_run_noalloc.argtypes = [vp, i64, i64, C.c_uint32, vp, vp]
     L.egsgpu_reset.argtypes = [vp]
+    L.egsgpu_adjoint.argtypes = [vp, i64, i64, C.c_uint32, dp, dp]
+    L.egsgpu_set_phantoms.argtypes = [vp, C.c_int, C.POINTER(PhantomStruct)]
+    L.egsgpu_run_phantoms.argtypes = [vp, C.c_int, vp]
+    L.egsgpu_get_phantom_dose.argtypes = [vp, C.c_int, dp, dp]
+    L.egsgpu_get_phantom_info.argtypes = [vp, C.c_int, C.POINTER(C.c_longlong)]
     L.egsgpu_get_tallies.argtypes = [vp, dp, dp, dp]
     L.egsgpu_get_dose.argtypes = [vp, dp, dp]
     L.egsgpu_get_profile.argtypes = [vp, dp]
@@ -146,6 +152,34 @@ class ParallelBeam:
             self.s.energy = float(self._edges[-1])
 
 
+class PhantomStruct(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("xb", C.POINTER(C.c_double)), ("yb", C.POINTER(C.c_double)), ("zb", C.POINTER(C.c_double)),
+                ("med", C.POINTER(C.c_int32)), ("rhor", C.POINTER(C.c_double)),
+                ("source", SourceStruct), ("seed", C.c_uint32), ("histories", C.c_longlong)]
+
+
+class PhaseSpaceSource:
+    """EGS_PhspSource / DOSXYZnrc isource 2: particles read from a phase-space
+    file (formats.read_egsphsp) or given as an (n, 7) float32 array of
+    {charge, kinetic energy (MeV), x, y, u, v, weight} (a negative weight
+    means w < 0), placed in the plane z = position[2] and shifted by
+    position[0], position[1].  Each particle is used recycle + 1 times with
+    its weight shared."""
+
+    def __init__(self, particles, position=(0.0, 0.0, 0.0), recycle=0):
+        self._p = np.ascontiguousarray(particles, dtype=np.float32).reshape(-1, 7)
+        self.s = SourceStruct()
+        self.s.shape = 2
+        self.s.pos[:] = tuple(float(v) for v in position)
+        self.s.dir[:] = (0.0, 0.0, 1.0)
+        self.s.nphsp = len(self._p)
+        self.s.phsp = self._p.ctypes.data_as(C.POINTER(C.c_float))
+        self.s.recycle = int(recycle)
+        self.s.energy = float(self._p[:, 1].max())
+        self.s.charge = -1 if np.any(self._p[:, 0] != 0) else 0
+
+
 def default_config(**kw):
     cfg = Config()
     load_library().egsgpu_default_config(C.byref(cfg))
@@ -203,8 +237,58 @@ class DoseEngine:
     def reset(self):
         self._check(self.L.egsgpu_reset(self.h))
 
+    def adjoint(self, dL_dD, n, seed=1, first=0):
+        """dL/d(rhor) per voxel for a loss of the dose of the run held in the
+        tallies (histories [first, first+n) with `seed` since the last reset),
+        given dL/dD per voxel (egsgpu_adjoint)."""
+        g = np.ascontiguousarray(dL_dD, dtype=np.float64).ravel()
+        out = np.zeros_like(g)
+        self._check(self.L.egsgpu_adjoint(self.h, int(first), int(n), int(seed), _dp(g), _dp(out)))
+        return out
+
+    def set_phantoms(self, phantoms):
+        """Several independent problems run together (egsgpu_set_phantoms):
+        `phantoms` is a list of dicts with geometry (XYZGeometry), source
+        (ParallelBeam), seed and histories (per egsgpu_run_phantoms call)."""
+        arr = (PhantomStruct * len(phantoms))()
+        for a, ph in zip(arr, phantoms):
+            g = ph["geometry"]
+            a.nx, a.ny, a.nz = g.nx, g.ny, g.nz
+            a.xb, a.yb, a.zb = _dp(g.xb), _dp(g.yb), _dp(g.zb)
+            a.med = g.med.ctypes.data_as(C.POINTER(C.c_int32))
+            a.rhor = _dp(g.rhor)
+            a.source = ph["source"].s
+            a.seed = int(ph["seed"])
+            a.histories = int(ph["histories"])
+        self._check(self.L.egsgpu_set_phantoms(self.h, len(phantoms), arr))
+        self.phantoms = [ph["geometry"] for ph in phantoms]
+        self.geom = None
+        self._nvox_all = sum(g.nvox for g in self.phantoms)
+
+    def run_phantoms(self, nbatch=10, stream=None):
+        st = C.c_void_p(stream) if stream else None
+        self._check(self.L.egsgpu_run_phantoms(self.h, int(nbatch), st))
+
+    def phantom_info(self, k):
+        """(first global voxel index, voxels, histories run) of phantom k."""
+        o = (C.c_longlong * 3)()
+        self._check(self.L.egsgpu_get_phantom_info(self.h, int(k), o))
+        return int(o[0]), int(o[1]), int(o[2])
+
+    def phantom_dose(self, k):
+        nv = self.phantoms[k].nvox
+        d, s = np.zeros(nv), np.zeros(nv)
+        self._check(self.L.egsgpu_get_phantom_dose(self.h, int(k), _dp(d), _dp(s)))
+        return d, s
+
+    def phantom_tallies(self, k):
+        """Energy-deposit sum and sum of squares (MeV) of phantom k's voxels."""
+        s, s2, _ = self.tallies()
+        off, nv, _ = self.phantom_info(k)
+        return s[off:off + nv], s2[off:off + nv]
+
     def tallies(self):
-        nv = self.geom.nvox
+        nv = self.geom.nvox if self.geom is not None else self._nvox_all
         s, s2, t = np.zeros(nv), np.zeros(nv), np.zeros(8)
         self._check(self.L.egsgpu_get_tallies(self.h, _dp(s), _dp(s2), _dp(t)))
         return s, s2, t

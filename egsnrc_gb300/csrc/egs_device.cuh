@@ -53,13 +53,17 @@ struct Tables {
 };
 
 // ------------------------------------------------------------ geometry ----
+// One XYZ phantom.  Voxel indices are global: a run of several phantoms
+// places phantom k's voxels at [voff, voff + nx*ny*nz) of shared medium,
+// density and tally arrays (voff = 0 for a single phantom).
 template <class Real>
 struct Geom {
     int nx, ny, nz, nxy;
     const Real *xb, *yb, *zb;
-    const uint8_t *med;
+    const uint8_t *med;   // global arrays, indexed by the global voxel index
     const Real *rhor;
     Real bt, hbt;         // boundary tolerance (egs++/egs_functions.h:80-88)
+    int voff;             // global index of this phantom's first voxel
 };
 
 // ------------------------------------------------------------- source ----
@@ -69,6 +73,9 @@ struct Source {
     const double *edges;  // device
     const double *wi;     // device alias weights
     const int *bin;       // device alias bins
+    long long nphsp;      // shape 2: phase-space particles (device, 7 floats each)
+    const float *phsp;
+    int recycle;
 };
 
 // -------------------------------------------------------------- queues ----

@@ -10,6 +10,7 @@ template <class Real>
 struct Particle {
     Real x, y, z, u, v, w, E, wt;
     int ir, iq;
+    int pb;       // phantom of a multi-phantom run (derived from ir; not stored in queues)
     Rng rng;
 };
 
@@ -509,11 +510,17 @@ __device__ inline void msdist_pII(const Tables<Real> &T, const MedScalars<Real> 
     Real xi = q1 * lambda;
     MsState<Real> st;
     st.find_index = true; st.i = 0; st.j = 0; st.omega2 = 0;
-    Real w1, sint1, w2, sint2;
-    mscat(T, p.rng, lambda, chia2, xi, st, w1, sint1, err);
-    Azim<Real> a1 = azimuth<Real>(p.rng, err);
-    mscat(T, p.rng, lambda, chia2, xi, st, w2, sint2, err);
-    Azim<Real> a2 = azimuth<Real>(p.rng, err);
+    // the two half-step deflections share one copy of the sampling code
+    // (same random-number order: mscat, azimuth, mscat, azimuth)
+    Real w1 = 0, sint1 = 0, w2 = 0, sint2 = 0;
+    Azim<Real> a1{0, 0}, a2{0, 0};
+#pragma unroll 1
+    for (int half = 0; half < 2; ++half) {
+        Real wh, sh;
+        mscat(T, p.rng, lambda, chia2, xi, st, wh, sh, err);
+        Azim<Real> ah = azimuth<Real>(p.rng, err);
+        if (half == 0) { w1 = wh; sint1 = sh; a1 = ah; } else { w2 = wh; sint2 = sh; a2 = ah; }
+    }
     Real cphi1 = a1.c, sphi1 = a1.s, cphi2 = a2.c, sphi2 = a2.s;
     Real u2 = sint2 * cphi2, v2 = sint2 * sphi2, u2p = w1 * u2 + sint1 * w2;
     us = u2p * cphi1 - v2 * sphi1;

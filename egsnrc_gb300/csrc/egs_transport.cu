@@ -65,6 +65,22 @@ struct Params {
     Geom<Real> G;
     Queue<Real> pin, ein, pout, eout;    // consumed / produced queues
     double *dose;                         // batch tally per voxel
+    // several phantoms in one run (Multi kernels): per-phantom geometry,
+    // Philox seed and source, the phantoms' first global voxel indices
+    // (nprob + 1 entries, ascending) and, for the current batch, the prefix
+    // sums of the phantoms' history counts and their first history indices
+    const Geom<Real> *probs;
+    const uint32_t *pseeds;
+    const Source *psrc;
+    const int *pvoff;
+    const long long *pprefix, *pfirst;
+    int nprob;
+    // seed-replay adjoint: dL/dE per voxel (also weights the per-history
+    // tally when set), per-history weighted deposits G_h of the replayed
+    // histories (index hist - hist_first) and the dL/d(rhor) accumulator
+    const double *wvox;
+    const double *hist_G;
+    double *grad;
     double *hist_tally;                   // optional per-history deposits
     long long hist_first, hist_n;
     double *energy;                       // [0] deposited, [1] escaped
@@ -97,7 +113,7 @@ __device__ inline void acc_flush(const Params<Real> &P, Acc<Real> &a) {
         atomicAdd(P.dose + a.ir, (double)a.e);
         if (P.hist_tally) {
             long long i = (long long)a.hist - P.hist_first;
-            if (i >= 0 && i < P.hist_n) atomicAdd(P.hist_tally + i, (double)a.e);
+            if (i >= 0 && i < P.hist_n) atomicAdd(P.hist_tally + i, P.wvox ? P.wvox[a.ir] * (double)a.e : (double)a.e);
         }
     }
     a.e = 0;
@@ -112,6 +128,62 @@ __device__ inline void deposit(const Params<Real> &P, Acc<Real> &a, int ir, uint
         a.hist = hist;
     }
     a.e += e;
+}
+
+// Gradient contributions of one particle's visit to one voxel, flushed with
+// one FP64 atomic when the voxel changes (adjoint replay only).
+template <class Real>
+struct AccG {
+    int ir;
+    Real g;
+};
+template <class Real>
+__device__ inline void gflush(const Params<Real> &P, AccG<Real> &a) {
+    if (a.ir >= 0 && a.g != 0) atomicAdd(P.grad + a.ir, (double)a.g);
+    a.g = 0;
+    a.ir = -1;
+}
+template <class Real>
+__device__ inline void gadd(const Params<Real> &P, AccG<Real> &a, int ir, Real g) {
+    if (ir != a.ir) {
+        gflush(P, a);
+        a.ir = ir;
+    }
+    a.g += g;
+}
+// Pathwise term of an electron's continuous energy loss.  With the random
+// numbers of a condensed-history step fixed in energy-loss units, the energy
+// lost inside voxel v scales with its density: d(de)/d(rhor_v) = de/rhor_v,
+// and the same energy is missing where the track ends (the voxel of its
+// cut-off deposit; nothing for a track that leaves the phantom or
+// annihilates).  ELIST voxel visits are kept per electron; a longer track is
+// closed early at its current voxel.
+constexpr int ELIST = 48;
+template <class Real>
+struct EList {
+    int n;
+    int v[ELIST];
+    Real a[ELIST];
+};
+template <class Real>
+__device__ inline void elist_close(const Params<Real> &P, EList<Real> &L, Real w_end) {
+    for (int i = 0; i < L.n; ++i)
+        if (L.a[i] != 0) atomicAdd(P.grad + L.v[i], -(double)(w_end * L.a[i]));
+    L.n = 0;
+}
+template <class Real>
+__device__ inline void elist_add(const Params<Real> &P, EList<Real> &L, int ir, Real a) {
+    if (L.n > 0 && L.v[L.n - 1] == ir) { L.a[L.n - 1] += a; return; }
+    if (L.n == ELIST) elist_close(P, L, (Real)P.wvox[ir]);
+    L.v[L.n] = ir;
+    L.a[L.n] = a;
+    ++L.n;
+}
+// G_h of the particle's history in an adjoint replay
+template <class Real>
+__device__ inline Real hist_weight(const Params<Real> &P, const Particle<Real> &p) {
+    long long i = (long long)p.rng.hist - P.hist_first;
+    return (i >= 0 && i < P.hist_n) ? (Real)P.hist_G[i] : (Real)0;
 }
 
 // ------------------------------------------------------------- queues ----
@@ -131,6 +203,33 @@ __device__ inline void q_load(const Queue<Real> &q, unsigned i, uint32_t seed, P
     p.E = q.E[i]; p.wt = q.wt[i]; p.ir = q.ir[i];
     p.iq = q.iq ? (int)q.iq[i] : 0;
     p.rng.init(seed, q.hist[i], q.sid[i], q.n[i]);
+}
+// The phantom holding global voxel `ir` (largest k with pvoff[k] <= ir).
+template <class Real>
+__device__ inline int phantom_of(const Params<Real> &P, int ir) {
+    int lo = 0, hi = P.nprob;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (ir >= P.pvoff[mid]) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+// Loads queue record i; in a multi-phantom run the particle's phantom (and
+// with it its Philox seed) follows from its voxel index.
+template <class Real, bool Multi>
+__device__ inline void load_particle(const Params<Real> &P, const Queue<Real> &q, unsigned i, Particle<Real> &p) {
+    if (Multi) {
+        int k = phantom_of(P, q.ir[i]);
+        q_load(q, i, P.pseeds[k], p);
+        p.pb = k;
+    } else {
+        q_load(q, i, P.seed, p);
+        p.pb = 0;
+    }
+}
+template <class Real, bool Multi>
+__device__ inline const Geom<Real> &geom_of(const Params<Real> &P, int pb) {
+    return Multi ? P.probs[pb] : P.G;
 }
 // Warp-aggregated append: the lanes that reach the push together share one
 // atomic on the queue counter.  Returns the slot, or ~0u when the queue is full.
@@ -167,7 +266,7 @@ __device__ inline void annih_at_rest(const Params<Real> &P, const Queue<Real> &q
     Azim<Real> az = azimuth<Real>(p.rng, err);
     Particle<Real> g1 = p, g2 = p;
     g1.E = rm; g1.iq = 0; g1.u = sinthe * az.c; g1.v = sinthe * az.s; g1.w = costhe;
-    g2.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
+    g2.rng.init(p.rng.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
     g2.E = rm; g2.iq = 0; g2.u = -g1.u; g2.v = -g1.v; g2.w = -g1.w;
     q_push(P, qp, g1, npush);
     q_push(P, qp, g2, npush);
@@ -195,7 +294,8 @@ __device__ inline void push_charged(const Params<Real> &P, const Queue<Real> &qe
 template <class Real>
 __device__ inline int howfar(const Geom<Real> &G, int ireg, Real x, Real y, Real z, Real u, Real v, Real w,
                              Real &t) {
-    int iz = ireg / G.nxy, ir = ireg - iz * G.nxy, iy = ir / G.nx, ix = ir - iy * G.nx;
+    const int loc = ireg - G.voff;
+    int iz = loc / G.nxy, ir = loc - iz * G.nxy, iy = ir / G.nx, ix = ir - iy * G.nx;
     int inew = ireg;
     if (u > 0) {
         Real d = (G.xb[ix + 1] - x) / u;
@@ -223,7 +323,8 @@ __device__ inline int howfar(const Geom<Real> &G, int ireg, Real x, Real y, Real
 // EGS_XYZGeometry::hownear (egs_nd_geometry.h:1106-1122)
 template <class Real>
 __device__ inline Real hownear(const Geom<Real> &G, int ireg, Real x, Real y, Real z) {
-    int iz = ireg / G.nxy, ir = ireg - iz * G.nxy, iy = ir / G.nx, ix = ir - iy * G.nx;
+    const int loc = ireg - G.voff;
+    int iz = loc / G.nxy, ir = loc - iz * G.nxy, iy = ir / G.nx, ix = ir - iy * G.nx;
     Real t = dmin(x - G.xb[ix], G.xb[ix + 1] - x);
     t = dmin(t, dmin(y - G.yb[iy], G.yb[iy + 1] - y));
     t = dmin(t, dmin(z - G.zb[iz], G.zb[iz + 1] - z));
@@ -241,21 +342,51 @@ __device__ inline int plane_where(const Real *b, int n, Real x) {
 }
 
 // ------------------------------------------------------------- source ----
-template <class Real>
-__global__ void k_source(Params<Real> P, Source S, long long first, long long n) {
+// One thread per history.  A single-phantom run transports histories
+// first + t; a multi-phantom run maps t to phantom k and history
+// pfirst[k] + (first + t - pprefix[k]) of that phantom, so every phantom sees
+// the histories (and random numbers) of a run of its own.
+template <class Real, bool Multi>
+__global__ void k_source(Params<Real> P, Source S0, long long first, long long n) {
     long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= n) return;
-    uint32_t hist = (uint32_t)(first + t);
+    int k = 0;
+    uint32_t hist = (uint32_t)(first + t), seed = P.seed;
+    if (Multi) {
+        long long g = first + t;
+        int lo = 0, hi = P.nprob;
+        while (hi - lo > 1) {
+            int mid = (lo + hi) >> 1;
+            if (g >= P.pprefix[mid]) lo = mid; else hi = mid;
+        }
+        k = lo;
+        hist = (uint32_t)(P.pfirst[k] + (g - P.pprefix[k]));
+        seed = P.pseeds[k];
+    }
+    const Source &S = Multi ? P.psrc[k] : S0;
     Particle<Real> p;
-    p.rng.init(P.seed, hist, 0ull, 0u);
+    p.rng.init(seed, hist, 0ull, 0u);
+    p.pb = k;
     p.wt = 1;
     double x = S.pos[0], y = S.pos[1], z = S.pos[2];
+    double u = S.dir[0], v = S.dir[1], w = S.dir[2];
+    int charge = S.charge;
     if (S.shape == 1) {
         x = S.xmin + (S.xmax - S.xmin) * (double)urand<Real>(p.rng);
         y = S.ymin + (S.ymax - S.ymin) * (double)urand<Real>(p.rng);
     }
     double ek;
-    if (S.spectrum == 0) ek = S.energy;
+    if (S.shape == 2) {   // phase-space particle (egs_phsp_source.cpp:296-320)
+        const float *q = S.phsp + 7 * (((long long)hist / (S.recycle + 1)) % S.nphsp);
+        charge = (int)q[0];
+        ek = q[1];
+        x += q[2]; y += q[3];
+        u = q[4]; v = q[5];
+        double a = u * u + v * v;
+        w = a < 1 ? sqrt(1 - a) : 0.0;
+        if (q[6] < 0) w = -w;
+        p.wt = (Real)(fabs((double)q[6]) / (S.recycle + 1));
+    } else if (S.spectrum == 0) ek = S.energy;
     else {
         double aj = (double)urand<Real>(p.rng) * S.nbins;
         int j = (int)aj;
@@ -263,13 +394,12 @@ __global__ void k_source(Params<Real> P, Source S, long long first, long long n)
         if (aj > S.wi[j]) j = S.bin[j];
         ek = S.edges[j] + (S.edges[j + 1] - S.edges[j]) * (double)urand<Real>(p.rng);
     }
-    p.iq = S.charge;
+    p.iq = charge;
     p.E = (Real)(p.iq == 0 ? ek : ek + RM);
-    double u = S.dir[0], v = S.dir[1], w = S.dir[2];
-    const Geom<Real> &G = P.G;
+    const Geom<Real> &G = geom_of<Real, Multi>(P, k);
     // isWhere, then howfarFromOut (egs_nd_geometry.h:1281-1379), in FP64
     int ix = plane_where(G.xb, G.nx, (Real)x), iy = plane_where(G.yb, G.ny, (Real)y), iz = plane_where(G.zb, G.nz, (Real)z);
-    int ir = (ix >= 0 && iy >= 0 && iz >= 0) ? ix + iy * G.nx + iz * G.nxy : -1;
+    int ir = (ix >= 0 && iy >= 0 && iz >= 0) ? G.voff + ix + iy * G.nx + iz * G.nxy : -1;
     if (ir < 0) {
         const Real *pl[3] = {G.xb, G.yb, G.zb};
         int nn[3] = {G.nx, G.ny, G.nz};
@@ -289,7 +419,7 @@ __global__ void k_source(Params<Real> P, Source S, long long first, long long n)
                 if (idx[c] < 0) { ok = false; break; }
             }
             if (!ok) continue;
-            int inew = idx[0] + idx[1] * G.nx + idx[2] * G.nxy;
+            int inew = G.voff + idx[0] + idx[1] * G.nx + idx[2] * G.nxy;
             if (t1 < (double)G.bt) {
                 Real tt = (Real)t1;
                 int itest = howfar(G, inew, (Real)q[0], (Real)q[1], (Real)q[2], (Real)u, (Real)v, (Real)w, tt);
@@ -317,7 +447,12 @@ struct PhotonState {
     int lgle;
 };
 
-template <class Real>
+// Adj: adjoint replay.  Each photon path segment of dpmfp mean free paths in
+// voxel v adds -G_h * dpmfp / rhor_v to dL/d(rhor_v) and each interaction in
+// v adds G_h / rhor_v: the score of the path's likelihood (all attenuation
+// coefficients scale with rhor, PHOTON's GMFP = GMFPR0 / RHOF), times the
+// history's weighted deposit G_h.
+template <class Real, bool Multi, bool Adj = false>
 __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
     const Tables<Real> &T = P.T;
     const Geom<Real> &G = P.G;
@@ -329,6 +464,8 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
     Particle<Real> p;
     PhotonState<Real> s;
     Acc<Real> acc{-1, 0u, (Real)0};
+    AccG<Real> ga{-1, (Real)0};
+    Real Gh = 0;
     bool alive = false, exhausted = false;
     unsigned long long nstep = 0, npush = 0, ninter = 0, lanes = 0, iters = 0;
     int inter_wait = 0;   // warp-uniform iterations since the first lane became due
@@ -360,7 +497,8 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
             if (!alive) {
                 unsigned idx = base + __popc(need & ((1u << lane) - 1u));
                 if (idx < nq) {
-                    q_load(P.pin, idx, P.seed, p);
+                    load_particle<Real, Multi>(P, P.pin, idx, p);
+                    if (Adj) Gh = hist_weight(P, p);
                     alive = true;
                     s.state = 0;
                     s.nsteps = 0;
@@ -402,6 +540,7 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
                 if (alive && s.state == 3) {
                 // interaction
                 ++ninter;
+                if (Adj) gadd(P, ga, p.ir, Gh / s.rhor);
                 const MedScalars<Real> &M = cmed<Real>(s.medium);
                 const Real *g = T.gtab + ((size_t)M.gtab_off + s.lgle - 1) * 8;
                 Real r37 = urand<Real>(p.rng);
@@ -422,7 +561,7 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
                     pair(M, p, E2, iq2, u2, v2, w2, err);
                     Particle<Real> q = p;
                     q.E = E2; q.iq = iq2; q.u = u2; q.v = v2; q.w = w2;
-                    q.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
+                    q.rng.init(p.rng.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
                     push_charged(P, P.ein, P.pout, p, acc, npush, edep_tot, err);
                     push_charged(P, P.ein, P.pout, q, acc, npush, edep_tot, err);
                     alive = false;
@@ -433,7 +572,7 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
                     Particle<Real> e = p;
                     Real edep = compton(T, M, p, e.u, e.v, e.w, e.E, err);
                     e.iq = -1;
-                    e.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
+                    e.rng.init(p.rng.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
                     if (edep > 0) { deposit(P, acc, p.ir, p.rng.hist, edep * p.wt); edep_tot += (double)(edep * p.wt); }
                     push_charged(P, P.ein, P.pout, e, acc, npush, edep_tot, err);
                     s.state = 0;
@@ -475,8 +614,9 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
         if (++s.nsteps > STEP_CAP) { err = 1; alive = false; continue; }
         Real gmfp = s.gmfpr0 / s.rhor * s.cohfac;
         Real ustep = gmfp * s.dpmfp;
-        int irnew = howfar(G, p.ir, p.x, p.y, p.z, p.u, p.v, p.w, ustep);
+        int irnew = howfar(geom_of<Real, Multi>(P, p.pb), p.ir, p.x, p.y, p.z, p.u, p.v, p.w, ustep);
         ++nstep;
+        if (Adj) gadd(P, ga, p.ir, -Gh * (ustep / gmfp) / s.rhor);
         p.x += p.u * ustep; p.y += p.v * ustep; p.z += p.w * ustep;
         s.dpmfp = dmax((Real)0, s.dpmfp - ustep / gmfp);
         if (irnew != p.ir) {
@@ -491,6 +631,7 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
         s.state = 3;   // interaction due: wait for the warp's batch
     }
     acc_flush(P, acc);
+    if (Adj) gflush(P, ga);
     // block-level counter reduction via warp shuffles
     for (int o = 16; o > 0; o >>= 1) {
         nstep += __shfl_down_sync(0xffffffffu, nstep, o);
@@ -581,7 +722,10 @@ __device__ inline Real eloss_g(const Tables<Real> &T, const MedScalars<Real> &M,
     return de + eke - eketmp;
 }
 
-template <class Real>
+// Adj: adjoint replay of the continuous energy loss (see EList); charged
+// secondaries go to the queue (no per-thread stack) so that every lane
+// follows one track at a time.
+template <class Real, bool Multi, bool Adj = false>
 __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
     const Tables<Real> &T = P.T;
     const Geom<Real> &G = P.G;
@@ -598,6 +742,9 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
     Particle<Real> lstack[LSTACK];
     int sp = 0;
     Acc<Real> acc{-1, 0u, (Real)0};
+    AccG<Real> ga{-1, (Real)0};
+    EList<Real> el;
+    el.n = 0;
     bool alive = false, exhausted = false;
     unsigned long long nstep = 0, npush = 0, ninter = 0, lanes = 0, iters = 0;
     int inter_wait = 0;   // warp-uniform iterations since the first lane became due
@@ -645,7 +792,8 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                 edep_part = 0;
                 unsigned idx = base + __popc(need & ((1u << lane) - 1u));
                 if (idx < nq) {
-                    q_load(P.ein, idx, P.seed, p);
+                    load_particle<Real, Multi>(P, P.ein, idx, p);
+                    if (Adj) el.n = 0;
                     alive = true;
                     s.state = 0;
                     s.nsteps = 0;
@@ -728,13 +876,13 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                             rotate(a, b, c, sinthe, costhe, az, p.u, p.v, p.w);
                             p.E = pese1;
                             Particle<Real> d = p;
-                            d.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
+                            d.rng.init(p.rng.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
                             dcosth = h1 * (pese2 - rm) / (pese2 + rm);
                             sinthe = -dsqrt(dmax((Real)0, 1 - dcosth));
                             costhe = dsqrt(dmin((Real)1, dcosth));
                             rotate(a, b, c, sinthe, costhe, az, d.u, d.v, d.w);
                             d.E = pese2; d.iq = -1;
-                            if (d.E > T.ecut && sp < LSTACK) { lstack[sp++] = p; p = d; }
+                            if (!Adj && d.E > T.ecut && sp < LSTACK) { lstack[sp++] = p; p = d; }
                             else push_charged(P, P.eout, P.pout, d, acc, npush, edep_tot, err);
                             s.state = 0;
                             continue;
@@ -770,13 +918,13 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                                 rotate(a, b, c, sinthe, costhe, az, p.u, p.v, p.w);
                                 p.E = pese1; p.iq = iq_np;
                                 Particle<Real> d = p;
-                                d.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
+                                d.rng.init(p.rng.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
                                 dcosth = h1 * (pese2 - rm) / (pese2 + rm);
                                 sinthe = -dsqrt(dmax((Real)0, 1 - dcosth));
                                 costhe = dsqrt(dmin((Real)1, dcosth));
                                 rotate(a, b, c, sinthe, costhe, az, d.u, d.v, d.w);
                                 d.E = pese2; d.iq = iq_new;
-                                if (d.E > T.ecut && sp < LSTACK) { lstack[sp++] = p; p = d; }
+                                if (!Adj && d.E > T.ecut && sp < LSTACK) { lstack[sp++] = p; p = d; }
                                 else push_charged(P, P.eout, P.pout, d, acc, npush, edep_tot, err);
                                 s.state = 0;
                                 continue;
@@ -800,7 +948,7 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                             Particle<Real> g1 = p, g2 = p;
                             g1.E = esg1; g1.iq = 0;
                             rotate(aa, bb, cc, sinthe, costhe, az, g1.u, g1.v, g1.w);
-                            g2.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
+                            g2.rng.init(p.rng.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
                             Real esg2 = pavip - esg1;
                             g2.E = esg2; g2.iq = 0;
                             costhe = dmax((Real)-1, dmin((Real)1, (esg2 - rm) * pot / esg2));
@@ -808,6 +956,7 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                             rotate(aa, bb, cc, sinthe, costhe, az, g2.u, g2.v, g2.w);
                             q_push(P, P.pout, g1, npush);
                             q_push(P, P.pout, g2, npush);
+                            if (Adj) elist_close(P, el, (Real)0);
                             alive = false;
                             continue;
                         }
@@ -869,7 +1018,7 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                         Real sinthe = dsqrt(dmax((1 - costhe) * (1 + costhe), (Real)0));
                         Azim<Real> az = azimuth<Real>(p.rng, err);
                         Particle<Real> gph = p;
-                        gph.rng.init(P.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
+                        gph.rng.init(p.rng.seed, p.rng.hist, child_sid(p.rng.sid, p.rng.n, 0), 0u);
                         gph.E = esg; gph.iq = 0;
                         if (sinpsi >= (Real)1e-10) {
                             Real us = sinthe * az.c, vs = sinthe * az.s;
@@ -951,7 +1100,8 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
             }
             tmxs = dmin(tmxs, T.smaxir);
             Real tustep = (Real)dmin(tstep, dmin((Real)tmxs, range));
-            Real tperp = hownear(G, p.ir, p.x, p.y, p.z);
+            const Geom<Real> &GP = geom_of<Real, Multi>(P, p.pb);
+            Real tperp = hownear(GP, p.ir, p.x, p.y, p.z);
             Real blccl = rhof * M.blcc;
             Real p2 = s.eke * (s.eke + 2 * rm), beta2 = p2 / (p2 + rm * rm);
             Real ssmfp = beta2 / blccl, skindepth = T.skindepth * ssmfp;
@@ -963,8 +1113,6 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
             if (tustep <= tperp && tustep > skindepth) {
                 callhowfar = false;
                 callmsdist = true;
-                de = eloss_g(T, M, qel, (Real)tustep, (Real)s.eke, (Real)s.elke, s.lelke, range, (Real)rhof);
-                msdist_pII(T, M, p, s.eke, (Real)de, tustep, rhof, uf, vf, wf, xf, yf, zf, err);
                 ustep = tustep;
             } else {
                 callmsdist = false;
@@ -986,13 +1134,14 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                 callhowfar = !(ustep < tperp);
             }
             int irold = p.ir, irnew = p.ir;
-            if (callhowfar) irnew = howfar(G, p.ir, p.x, p.y, p.z, p.u, p.v, p.w, ustep);
+            if (callhowfar) irnew = howfar(GP, p.ir, p.x, p.y, p.z, p.u, p.v, p.w, ustep);
             if (ustep <= 0) ustep = 0;
             if (ustep == 0) {
                 if (irnew != irold) {
                     p.ir = irnew;
                     if (irnew < 0) {
                         esc_tot += (double)((p.iq < 0 ? p.E - rm : p.E + rm) * p.wt);
+                        if (Adj) elist_close(P, el, (Real)0);
                         alive = false;
                         continue;
                     }
@@ -1003,15 +1152,10 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                 else { s.state = 1; continue; }
             }
             if (!ecut_discard) {
-                Real vstep = ustep, tvstep;
-                if (callhowfar) {
-                    tvstep = vstep;
-                    if (tvstep != tustep) dosingle = false;
-                    de = eloss_g(T, M, qel, (Real)tvstep, (Real)s.eke, (Real)s.elke, s.lelke, range, (Real)rhof);
-                } else {
-                    tvstep = tustep;
-                    if (!callmsdist) de = eloss_g(T, M, qel, (Real)tvstep, (Real)s.eke, (Real)s.elke, s.lelke, range, (Real)rhof);
-                }
+                Real vstep = ustep, tvstep = callhowfar ? vstep : tustep;
+                if (callhowfar && tvstep != tustep) dosingle = false;
+                de = eloss_g(T, M, qel, (Real)tvstep, (Real)s.eke, (Real)s.elke, s.lelke, range, (Real)rhof);
+                if (callmsdist) msdist_pII(T, M, p, s.eke, (Real)de, tustep, rhof, uf, vf, wf, xf, yf, zf, err);
                 Real edep = (Real)de, ekef = s.eke - edep;
                 if (!callmsdist) {
                     xf = p.x + p.u * vstep; yf = p.y + p.v * vstep; zf = p.z + p.w * vstep;
@@ -1027,6 +1171,11 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                     } else { uf = p.u; vf = p.v; wf = p.w; }
                 }
                 deposit(P, acc, p.ir, p.rng.hist, edep * p.wt);   // AUSGAB(0)
+                if (Adj && edep > 0) {
+                    Real a = edep * p.wt / s.rhor;
+                    gadd(P, ga, p.ir, (Real)P.wvox[p.ir] * a);
+                    elist_add(P, el, p.ir, a);
+                }
                 edep_part += edep * p.wt;
                 p.x = xf; p.y = yf; p.z = zf; p.u = uf; p.v = vf; p.w = wf;
                 p.E = p.E - edep;
@@ -1040,6 +1189,7 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                         p.ir = irnew;
                         if (irnew < 0) {
                             esc_tot += (double)((p.iq < 0 ? p.E - rm : p.E + rm) * p.wt);
+                            if (Adj) elist_close(P, el, (Real)0);
                             alive = false;
                             continue;
                         }
@@ -1072,11 +1222,13 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
             Real edep = p.E - rm;
             deposit(P, acc, p.ir, p.rng.hist, edep * p.wt);
             edep_tot += (double)(edep * p.wt);
+            if (Adj) elist_close(P, el, (Real)P.wvox[p.ir]);
             if (p.iq > 0) annih_at_rest(P, P.pout, p, npush, err);
             alive = false;
         }
     }
     acc_flush(P, acc);
+    if (Adj) gflush(P, ga);
     edep_tot += (double)edep_part;
     for (int o = 16; o > 0; o >>= 1) {
         nstep += __shfl_down_sync(0xffffffffu, nstep, o);
@@ -1138,6 +1290,16 @@ struct DevMem {
     }
 };
 
+// One phantom of a multi-phantom run, as handed to the engine.
+struct PhantomDesc {
+    int nx, ny, nz;
+    const double *xb, *yb, *zb;
+    const int32_t *med;
+    const double *rhor;
+    uint32_t seed;
+    long long histories;
+};
+
 struct EngineBase {
     virtual ~EngineBase() {}
     virtual int load(const egs::Hatch &H, double ecut, double pcut, double skindepth, std::string &err) = 0;
@@ -1147,6 +1309,10 @@ struct EngineBase {
                     std::string &err) = 0;
     virtual int run_noalloc(const Source &S, long long first, long long n, uint32_t seed, double *dose,
                             cudaStream_t st, unsigned char *scratch, size_t scratch_bytes, std::string &err) = 0;
+    virtual int problems(int n, const PhantomDesc *pd, const Source *src, std::string &err) = 0;
+    virtual int run_multi(const Source &Smax, int nbatch, cudaStream_t st, std::string &err) = 0;
+    virtual int adjoint(const Source &S, long long first, long long n, uint32_t seed, const double *w, double *grad,
+                        std::string &err) = 0;
 };
 
 template <class Real>
@@ -1312,6 +1478,7 @@ struct Engine : EngineBase {
 
     int geometry(int nx, int ny, int nz, const double *xb, const double *yb, const double *zb, const int32_t *med,
                  const double *rhor, std::string &err) override {
+        nprob = 0;
         nvox = (long long)nx * ny * nz;
         std::vector<Real> x(xb, xb + nx + 1), y(yb, yb + ny + 1), z(zb, zb + nz + 1), r(nvox);
         std::vector<uint8_t> m(nvox);
@@ -1332,6 +1499,7 @@ struct Engine : EngineBase {
         // egs++ distanceEpsilon: 2^-32 cm in FP64, 2^-21 cm in FP32 (egs++/egs_functions.h:80-88)
         G.bt = sizeof(Real) == 8 ? (Real)(1.0 / 4294967296.0) : (Real)(1.0 / 2097152.0);
         G.hbt = G.bt / 2;
+        G.voff = 0;
         CK(d_dose.alloc(nvox * sizeof(double)));
         CK(d_sum.alloc(nvox * sizeof(double)));
         CK(d_sum2.alloc(nvox * sizeof(double)));
@@ -1384,7 +1552,7 @@ struct Engine : EngineBase {
     cudaEvent_t ev_in = nullptr;
     bool graph_ok = true;
 
-    cudaError_t enqueue_rounds(const Params<Real> &P0, int grid, int bs, bool events) {
+    cudaError_t enqueue_rounds(const Params<Real> &P0, int grid, int bs, bool events, bool multi, bool adj = false) {
         unsigned *counts = (unsigned *)d_counts.p;
         cudaError_t e = cudaSuccess;
         for (int r = 0; r < ROUNDS && e == cudaSuccess; ++r) {
@@ -1394,11 +1562,15 @@ struct Engine : EngineBase {
             if ((e = cudaMemsetAsync(counts + 2 * nxt, 0, 2 * sizeof(unsigned), ws))) break;
             if ((e = cudaMemsetAsync(counts + 4 + 2 * nxt, 0, 2 * sizeof(unsigned), ws))) break;
             if (events && (e = cudaEventRecord(gev[4 * r], ws))) break;
-            k_photon<Real><<<grid, bs, 0, ws>>>(P);
+            if (adj) k_photon<Real, false, true><<<grid, bs, 0, ws>>>(P);
+            else if (multi) k_photon<Real, true><<<grid, bs, 0, ws>>>(P);
+            else k_photon<Real, false><<<grid, bs, 0, ws>>>(P);
             if ((e = cudaGetLastError())) break;
             if (events && (e = cudaEventRecord(gev[4 * r + 1], ws))) break;
             if (events && (e = cudaEventRecord(gev[4 * r + 2], ws))) break;
-            k_electron<Real><<<grid, bs, 0, ws>>>(P);
+            if (adj) k_electron<Real, false, true><<<grid, bs, 0, ws>>>(P);
+            else if (multi) k_electron<Real, true><<<grid, bs, 0, ws>>>(P);
+            else k_electron<Real, false><<<grid, bs, 0, ws>>>(P);
             if ((e = cudaGetLastError())) break;
             if (events && (e = cudaEventRecord(gev[4 * r + 3], ws))) break;
         }
@@ -1407,14 +1579,14 @@ struct Engine : EngineBase {
 
     // Captures the rounds (without events) into a graph; on any failure the
     // engine keeps launching directly.
-    void build_graph(const Params<Real> &P0, int grid, int bs) {
+    void build_graph(const Params<Real> &P0, int grid, int bs, bool multi) {
         if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
         if (cudaStreamBeginCapture(ws, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
             cudaGetLastError();
             graph_ok = false;
             return;
         }
-        cudaError_t e = enqueue_rounds(P0, grid, bs, false);
+        cudaError_t e = enqueue_rounds(P0, grid, bs, false, multi);
         cudaGraph_t g = nullptr;
         cudaError_t e2 = cudaStreamEndCapture(ws, &g);
         if (e == cudaSuccess && e2 == cudaSuccess && g) e = cudaGraphInstantiate(&gexec, g, 0);
@@ -1434,6 +1606,21 @@ struct Engine : EngineBase {
 
     int run(const Source &S, long long first, long long n, int nbatch, uint32_t seed, cudaStream_t st,
             std::string &err) override {
+        if (nprob) { err = "the engine holds several phantoms; set one geometry first"; return EGSGPU_ERR_STATE; }
+        return run_impl<false>(S, first, n, nbatch, seed, st, err);
+    }
+
+    // Histories of batch b of a run of n histories in nbatch batches
+    // (the same split for one phantom and for each phantom of many).
+    static void batch_range(long long first, long long n, int nbatch, int b, long long &b0, long long &bn) {
+        long long per = n / nbatch;
+        b0 = first + b * per;
+        bn = (b == nbatch - 1) ? n - b * per : per;
+    }
+
+    template <bool Multi>
+    int run_impl(const Source &S, long long first, long long n, int nbatch, uint32_t seed, cudaStream_t st,
+                 std::string &err) {
         if (!G.xb) { err = "geometry not set"; return EGSGPU_ERR_STATE; }
         unsigned cap = cfg.capacity > 0 ? (unsigned)std::min<long long>(cfg.capacity, 0x7fffffffLL) : (1u << 25);
         if (int rc = ensure_queues(cap, err)) return rc;
@@ -1462,14 +1649,21 @@ struct Engine : EngineBase {
         const int bs = cfg.block_size > 0 ? cfg.block_size : 128;
         // persistent grids: never more CTAs than can be resident at once
         int occ_p = 1, occ_e = 1;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real>, bs, 0));
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real>, bs, 0));
+        const bool adj = mode && mode->adj;
+        if (adj) {
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, false, true>, bs, 0));
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, false, true>, bs, 0));
+        } else {
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, Multi>, bs, 0));
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, Multi>, bs, 0));
+        }
         const int cps = std::max(1, std::min(cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm : 64, std::min(occ_p, occ_e)));
         const int grid = sm_count * cps;
         Params<Real> P;
+        std::memset(&P, 0, sizeof(P));
         P.T = T; P.G = G;
         P.dose = (double *)d_dose.p;
-        P.hist_tally = hist_n > 0 ? (double *)d_hist.p : nullptr;
+        P.hist_tally = (!Multi && hist_n > 0) ? (double *)d_hist.p : nullptr;
         P.hist_first = hist_first; P.hist_n = hist_n;
         P.energy = (double *)d_energy.p;
         P.counters = (unsigned long long *)d_counters.p;
@@ -1478,29 +1672,58 @@ struct Engine : EngineBase {
         P.seed = seed;
         P.requeue_lanes = cfg.requeue_lanes > 0 ? cfg.requeue_lanes : 0;
         P.inter_batch = cfg.inter_batch > 0 ? std::min(cfg.inter_batch, 32) : (cfg.inter_batch < 0 ? 1 : 12);
+        if (Multi) {
+            P.probs = (const Geom<Real> *)d_probs.p; P.pseeds = (const uint32_t *)d_pseeds.p;
+            P.psrc = (const Source *)d_psrc.p; P.pvoff = (const int *)d_pvoff.p;
+            P.pprefix = (const long long *)d_pprefix.p; P.pfirst = (const long long *)d_pfirst.p;
+            P.nprob = nprob;
+        }
+        if (mode) {   // a replay for the adjoint: its own tallies, never the run's
+            P.dose = mode->dose; P.energy = mode->energy; P.counters = mode->counters;
+            P.hist_tally = mode->hist; P.hist_first = mode->hist_first; P.hist_n = mode->hist_n;
+            P.wvox = mode->wvox; P.hist_G = mode->hist_G; P.grad = mode->grad;
+            P.requeue_lanes = 0;
+        }
         P.pin = q[0]; P.ein = q[2]; P.pout = q[0]; P.eout = q[2];
-        const bool use_graph = cfg.use_graph > 0 && graph_ok;
-        if (use_graph) build_graph(P, grid, bs);
+        const bool use_graph = cfg.use_graph > 0 && graph_ok && !mode;
+        if (use_graph) build_graph(P, grid, bs, Multi);
         const bool graph = use_graph && gexec;
         unsigned *counts = (unsigned *)d_counts.p;
         CK(cudaEventRecord(ev_in, st));
         CK(cudaStreamWaitEvent(ws, ev_in, 0));
-        long long per_batch = n / nbatch;
+        std::vector<long long> hprefix(nprob + 1), hfirst(nprob + 1);
         for (int b = 0; b < nbatch; ++b) {
-            long long b0 = first + b * per_batch, bn = (b == nbatch - 1) ? n - b * per_batch : per_batch;
+            long long b0, bn;
+            if (Multi) {
+                // batch b of every phantom, laid end to end
+                hprefix[0] = 0;
+                for (int k = 0; k < nprob; ++k) {
+                    long long f, c;
+                    batch_range(pdone[k], phist[k], nbatch, b, f, c);
+                    hfirst[k] = f;
+                    hprefix[k + 1] = hprefix[k] + c;
+                }
+                hfirst[nprob] = 0;
+                CK(cudaMemcpyAsync(d_pprefix.p, hprefix.data(), (nprob + 1) * sizeof(long long), cudaMemcpyHostToDevice, ws));
+                CK(cudaMemcpyAsync(d_pfirst.p, hfirst.data(), (nprob + 1) * sizeof(long long), cudaMemcpyHostToDevice, ws));
+                b0 = 0;
+                bn = hprefix[nprob];
+            } else {
+                batch_range(first, n, nbatch, b, b0, bn);
+            }
             for (long long c0 = b0, cn = 0; c0 < b0 + bn; c0 += cn) {
                 cn = std::min(chunk, b0 + bn - c0);   // the autotuner may change `chunk` below
                 auto t_chunk = std::chrono::steady_clock::now();
                 CK(cudaMemsetAsync(counts, 0, 9 * sizeof(unsigned), ws));
                 CK(cudaEventRecord(ev[0], ws));
-                k_source<Real><<<(unsigned)((cn + 255) / 256), 256, 0, ws>>>(P, S, c0, cn);
+                k_source<Real, Multi><<<(unsigned)((cn + 255) / 256), 256, 0, ws>>>(P, S, c0, cn);
                 CK(cudaGetLastError());
                 CK(cudaEventRecord(ev[1], ws));
                 unsigned h[9] = {};
                 bool done = false;
                 for (int rep = 0; rep < 100000 / ROUNDS && !done; ++rep) {
                     if (graph) CK(cudaGraphLaunch(gexec, ws));
-                    else CK(enqueue_rounds(P, grid, bs, true));
+                    else CK(enqueue_rounds(P, grid, bs, true, Multi, adj));
                     CK(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, ws));
                     CK(cudaStreamSynchronize(ws));
                     if (rep == 0) { prof_ms[0] += elapsed(ev[0], ev[1]); ++prof_n[0]; }
@@ -1538,6 +1761,7 @@ struct Engine : EngineBase {
                     }
                 }
             }
+            if (mode) { CK(cudaStreamSynchronize(ws)); continue; }
             CK(cudaEventRecord(ev[6], ws));
             k_batch<<<std::max(1, std::min(4 * sm_count, (int)((nvox + 255) / 256))), 256, 0, ws>>>(
                 (double *)d_dose.p, (double *)d_sum.p, (double *)d_sum2.p, nvox);
@@ -1555,12 +1779,146 @@ struct Engine : EngineBase {
         return 0;
     }
 
+    // ------------------------------------------------------- adjoint ----
+    // A replay of histories for the adjoint writes to scratch tallies, so the
+    // run being differentiated keeps its own.
+    struct RunMode {
+        bool adj;
+        double *dose, *energy;
+        unsigned long long *counters;
+        double *hist;
+        long long hist_first, hist_n;
+        const double *wvox, *hist_G;
+        double *grad;
+    };
+    const RunMode *mode = nullptr;
+    DevMem d_aw, d_agrad, d_aG, d_adose, d_aenergy, d_acount;
+
+    // dL/d(rhor) of the histories [first, first+n) for energy weights
+    // w_v = dL/dE_v: pass 1 replays the histories with weighted per-history
+    // tallies (G_h = sum of w_v * deposit over history h), pass 2 replays them
+    // again with the adjoint kernels, which add the photon path scores times
+    // G_h and the electrons' pathwise continuous-loss terms.
+    int adjoint(const Source &S, long long first, long long n, uint32_t seed, const double *w, double *grad,
+                std::string &err) override {
+        if (!G.xb || nprob) { err = "a single geometry must be set"; return EGSGPU_ERR_STATE; }
+        CK(d_aw.alloc(nvox * sizeof(double)));
+        CK(d_agrad.alloc(nvox * sizeof(double)));
+        CK(d_aG.alloc(n * sizeof(double)));
+        CK(d_adose.alloc(nvox * sizeof(double)));
+        CK(d_aenergy.alloc(2 * sizeof(double)));
+        CK(d_acount.alloc(CNT_N * sizeof(unsigned long long)));
+        CK(cudaMemcpy(d_aw.p, w, nvox * sizeof(double), cudaMemcpyHostToDevice));
+        CK(cudaMemset(d_agrad.p, 0, nvox * sizeof(double)));
+        CK(cudaMemset(d_aG.p, 0, n * sizeof(double)));
+        CK(cudaMemset(d_adose.p, 0, nvox * sizeof(double)));
+        CK(cudaMemset(d_aenergy.p, 0, 2 * sizeof(double)));
+        CK(cudaMemset(d_acount.p, 0, CNT_N * sizeof(unsigned long long)));
+        RunMode m{false, (double *)d_adose.p, (double *)d_aenergy.p, (unsigned long long *)d_acount.p,
+                  (double *)d_aG.p, first, n, (const double *)d_aw.p, nullptr, nullptr};
+        mode = &m;
+        int rc = run_impl<false>(S, first, n, 1, seed, nullptr, err);
+        if (!rc) {
+            m = RunMode{true, (double *)d_adose.p, (double *)d_aenergy.p, (unsigned long long *)d_acount.p,
+                        nullptr, first, n, (const double *)d_aw.p, (const double *)d_aG.p, (double *)d_agrad.p};
+            rc = run_impl<false>(S, first, n, 1, seed, nullptr, err);
+        }
+        mode = nullptr;
+        if (rc) return rc;
+        CK(cudaMemcpy(grad, d_agrad.p, nvox * sizeof(double), cudaMemcpyDeviceToHost));
+        return 0;
+    }
+
+    // ------------------------------------------------ several phantoms ----
+    // The phantoms' planes, media and densities are laid end to end in the
+    // engine's geometry buffers (phantom k's voxels at global indices
+    // [voff_k, voff_k+1)), so the tallies, the batch fold and the read-back
+    // serve all phantoms at once.
+    int nprob = 0;
+    std::vector<long long> phist;   // histories per phantom per run
+    std::vector<long long> pdone;   // histories already transported per phantom
+    DevMem d_probs, d_pseeds, d_psrc, d_pvoff, d_pprefix, d_pfirst;
+
+    int problems(int n, const PhantomDesc *pd, const Source *src, std::string &err) override {
+        std::vector<Real> x, y, z, r;
+        std::vector<uint8_t> m;
+        std::vector<int> voff(n + 1, 0);
+        std::vector<long long> xo(n), yo(n), zo(n);
+        long long tot = 0;
+        for (int k = 0; k < n; ++k) {
+            const PhantomDesc &d = pd[k];
+            long long nv = (long long)d.nx * d.ny * d.nz;
+            if (tot + nv > 0x7fffffffLL) { err = "too many voxels over all phantoms"; return EGSGPU_ERR_ARG; }
+            voff[k] = (int)tot;
+            xo[k] = (long long)x.size(); yo[k] = (long long)y.size(); zo[k] = (long long)z.size();
+            x.insert(x.end(), d.xb, d.xb + d.nx + 1);
+            y.insert(y.end(), d.yb, d.yb + d.ny + 1);
+            z.insert(z.end(), d.zb, d.zb + d.nz + 1);
+            for (long long i = 0; i < nv; ++i) { m.push_back((uint8_t)d.med[i]); r.push_back((Real)d.rhor[i]); }
+            tot += nv;
+        }
+        voff[n] = (int)tot;
+        auto up = [&](DevMem &dm, const void *p, size_t bytes) -> cudaError_t {
+            cudaError_t e = dm.alloc(bytes);
+            if (e != cudaSuccess) return e;
+            return cudaMemcpy(dm.p, p, bytes, cudaMemcpyHostToDevice);
+        };
+        CK(up(d_xb, x.data(), x.size() * sizeof(Real)));
+        CK(up(d_yb, y.data(), y.size() * sizeof(Real)));
+        CK(up(d_zb, z.data(), z.size() * sizeof(Real)));
+        CK(up(d_med, m.data(), m.size()));
+        CK(up(d_rhor, r.data(), r.size() * sizeof(Real)));
+        const Real bt = sizeof(Real) == 8 ? (Real)(1.0 / 4294967296.0) : (Real)(1.0 / 2097152.0);
+        std::vector<Geom<Real>> gs(n);
+        std::vector<uint32_t> seeds(n);
+        phist.assign(n, 0);
+        for (int k = 0; k < n; ++k) {
+            Geom<Real> &g = gs[k];
+            g.nx = pd[k].nx; g.ny = pd[k].ny; g.nz = pd[k].nz; g.nxy = g.nx * g.ny;
+            g.xb = (const Real *)d_xb.p + xo[k]; g.yb = (const Real *)d_yb.p + yo[k]; g.zb = (const Real *)d_zb.p + zo[k];
+            g.med = (const uint8_t *)d_med.p; g.rhor = (const Real *)d_rhor.p;
+            g.bt = bt; g.hbt = bt / 2;
+            g.voff = voff[k];
+            seeds[k] = pd[k].seed;
+            phist[k] = pd[k].histories;
+        }
+        CK(up(d_probs, gs.data(), n * sizeof(Geom<Real>)));
+        CK(up(d_pseeds, seeds.data(), n * sizeof(uint32_t)));
+        CK(up(d_psrc, src, n * sizeof(Source)));
+        CK(up(d_pvoff, voff.data(), (n + 1) * sizeof(int)));
+        CK(d_pprefix.alloc((n + 1) * sizeof(long long)));
+        CK(d_pfirst.alloc((n + 1) * sizeof(long long)));
+        G = gs[0];
+        nvox = tot;
+        nprob = n;
+        pdone.assign(n, 0);
+        CK(d_dose.alloc(nvox * sizeof(double)));
+        CK(d_sum.alloc(nvox * sizeof(double)));
+        CK(d_sum2.alloc(nvox * sizeof(double)));
+        CK(cudaMemset(d_dose.p, 0, nvox * sizeof(double)));
+        CK(cudaMemset(d_sum.p, 0, nvox * sizeof(double)));
+        CK(cudaMemset(d_sum2.p, 0, nvox * sizeof(double)));
+        return 0;
+    }
+
+    // Each call transports the next histories of every phantom: the first
+    // call histories [0, n_k), the second [n_k, 2 n_k), ...
+    int run_multi(const Source &Smax, int nbatch, cudaStream_t st, std::string &err) override {
+        if (!nprob) { err = "no phantoms set"; return EGSGPU_ERR_STATE; }
+        for (int k = 0; k < nprob; ++k)
+            if (pdone[k] + phist[k] > 0xffffffffLL) { err = "history index beyond 2^32"; return EGSGPU_ERR_ARG; }
+        int rc = run_impl<true>(Smax, 0, 0, nbatch, 0, st, err);
+        if (!rc)
+            for (int k = 0; k < nprob; ++k) pdone[k] += phist[k];
+        return rc;
+    }
+
     // Transport of one small chunk with every piece of scratch (queues,
     // counters, error flags) carved out of a caller-independent static device
     // array; all work goes to the caller's stream.  See egsgpu_run_noalloc.
     int run_noalloc(const Source &S, long long first, long long n, uint32_t seed, double *dose, cudaStream_t st,
                     unsigned char *scratch, size_t scratch_bytes, std::string &err) override {
-        if (!G.xb) { err = "geometry not set"; return EGSGPU_ERR_STATE; }
+        if (!G.xb || nprob) { err = "a single geometry must be set"; return EGSGPU_ERR_STATE; }
         // layout: 1 KiB of counters, then four queues of equal capacity
         unsigned *counts = (unsigned *)scratch;                          // 16 x unsigned
         double *energy = (double *)(scratch + 256);                      // 2 x double
@@ -1590,10 +1948,11 @@ struct Engine : EngineBase {
         if ((size_t)(b - scratch) > scratch_bytes) { err = "no-allocation scratch layout overflow"; return EGSGPU_ERR_STATE; }
         const int bs = 128;
         int occ_p = 1, occ_e = 1;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real>, bs, 0));
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real>, bs, 0));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, false>, bs, 0));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, false>, bs, 0));
         const int grid = sm_count * std::max(1, std::min(occ_p, occ_e));
         Params<Real> P;
+        std::memset(&P, 0, sizeof(P));
         P.T = T; P.G = G;
         P.dose = dose;
         P.hist_tally = nullptr; P.hist_first = 0; P.hist_n = 0;
@@ -1605,7 +1964,7 @@ struct Engine : EngineBase {
         CK(cudaMemsetAsync(scratch, 0, 1024, st));
         CK(cudaMemsetAsync(dose, 0, (size_t)nvox * sizeof(double), st));
         P.pout = Q[0]; P.eout = Q[2]; P.pin = Q[0]; P.ein = Q[2];
-        k_source<Real><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(P, S, first, n);
+        k_source<Real, false><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(P, S, first, n);
         CK(cudaGetLastError());
         int cur = 0;
         bool done = false;
@@ -1614,9 +1973,9 @@ struct Engine : EngineBase {
             CK(cudaMemsetAsync(counts + 2 * nxt, 0, 2 * sizeof(unsigned), st));
             CK(cudaMemsetAsync(counts + 4 + 2 * nxt, 0, 2 * sizeof(unsigned), st));
             P.pin = Q[cur]; P.ein = Q[2 + cur]; P.pout = Q[nxt]; P.eout = Q[2 + nxt];
-            k_photon<Real><<<grid, bs, 0, st>>>(P);
+            k_photon<Real, false><<<grid, bs, 0, st>>>(P);
             CK(cudaGetLastError());
-            k_electron<Real><<<grid, bs, 0, st>>>(P);
+            k_electron<Real, false><<<grid, bs, 0, st>>>(P);
             CK(cudaGetLastError());
             unsigned h[9];
             CK(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, st));
@@ -1649,16 +2008,30 @@ struct egsgpu_handle {
     std::vector<int32_t> med;
     // source
     Source S{};
-    DevMem d_edges, d_wi, d_bin;
+    DevMem d_edges, d_wi, d_bin, d_phsp;
     long long nhist = 0;
     int nbatch = 0;
     double ecut = 0, pcut = 0;
+    // several phantoms (egsgpu_set_phantoms): host copies for the dose
+    // normalisation, global voxel offsets, histories run per phantom
+    struct Phantom {
+        int nx, ny, nz;
+        std::vector<double> xb, yb, zb, rhor;
+        std::vector<int32_t> med;
+        long long voff, histories, nhist;
+    };
+    std::vector<Phantom> phantoms;
+    long long mvox = 0;
+    Source Smax{};
+    DevMem d_pedges, d_pwi, d_pbin, d_pphsp;
+    bool multi() const { return !phantoms.empty(); }
+    long long nvox() const { return multi() ? mvox : (long long)nx * ny * nz; }
 };
 
 template <class E>
 static int get_tallies_impl(egsgpu_handle *h, E *eng, double *sum, double *sum2, double *totals) {
     std::string &err = h->err;
-    long long nv = (long long)h->nx * h->ny * h->nz;
+    long long nv = h->nvox();
     if (sum) CK(cudaMemcpy(sum, eng->d_sum.p, nv * sizeof(double), cudaMemcpyDeviceToHost));
     if (sum2) CK(cudaMemcpy(sum2, eng->d_sum2.p, nv * sizeof(double), cudaMemcpyDeviceToHost));
     if (totals) {
@@ -1751,58 +2124,108 @@ int egsgpu_set_xyz_geometry(egsgpu_handle *h, int nx, int ny, int nz, const doub
     h->xb.assign(xb, xb + nx + 1); h->yb.assign(yb, yb + ny + 1); h->zb.assign(zb, zb + nz + 1);
     h->med.assign(med, med + nv); h->rhor.assign(rhor, rhor + nv);
     h->have_geom = true;
+    h->phantoms.clear();
     h->nhist = 0; h->nbatch = 0;
     return 0;
 }
 
-int egsgpu_set_source(egsgpu_handle *h, const egsgpu_source *s) {
-    if (!h || !s) return EGSGPU_ERR_ARG;
-    if (s->charge < -1 || s->charge > 1 || (s->shape != 0 && s->shape != 1) || (s->spectrum != 0 && s->spectrum != 1)) {
-        h->err = "unsupported source";
+}  // extern "C"
+
+// Checks a source description and builds its host form; a histogram spectrum
+// becomes a Walker alias table over its bins (egs++/egs_alias_table.cpp:117-263)
+// returned in edges / wi / bin (device pointers are filled in by the caller).
+static int build_source(const egsgpu_source *s, Source &S, std::vector<double> &edges, std::vector<double> &wi,
+                        std::vector<int> &bin, std::string &err) {
+    if (s->charge < -1 || s->charge > 1 || s->shape < 0 || s->shape > 2 || (s->spectrum != 0 && s->spectrum != 1)) {
+        err = "unsupported source";
         return EGSGPU_ERR_ARG;
     }
+    if (s->shape == 2) {   // phase-space particles: checked here, copied by the caller
+        if (s->nphsp < 1 || !s->phsp || s->recycle < 0) { err = "bad phase-space source"; return EGSGPU_ERR_ARG; }
+        S = Source{};
+        S.shape = 2;
+        for (int k = 0; k < 3; ++k) S.pos[k] = s->pos[k];
+        S.dir[2] = 1;
+        S.nphsp = s->nphsp;
+        S.recycle = s->recycle;
+        double emax = 0;
+        for (long long i = 0; i < s->nphsp; ++i) {
+            const float *q = s->phsp + 7 * i;
+            if (!(q[0] == -1.0f || q[0] == 0.0f || q[0] == 1.0f) || !(q[1] > 0) || !std::isfinite(q[1]) ||
+                !(q[4] * q[4] + q[5] * q[5] <= 1.0f + 1e-5f)) {
+                err = "bad phase-space particle " + std::to_string(i);
+                return EGSGPU_ERR_ARG;
+            }
+            emax = std::max(emax, (double)q[1]);
+            if (q[0] != 0) S.charge = -1;
+        }
+        S.energy = emax;
+        edges.clear(); wi.clear(); bin.clear();
+        return 0;
+    }
     double nrm = std::sqrt(s->dir[0] * s->dir[0] + s->dir[1] * s->dir[1] + s->dir[2] * s->dir[2]);
-    if (!(nrm > 0)) { h->err = "zero source direction"; return EGSGPU_ERR_ARG; }
-    Source S{};
+    if (!(nrm > 0)) { err = "zero source direction"; return EGSGPU_ERR_ARG; }
+    S = Source{};
     S.charge = s->charge; S.shape = s->shape; S.spectrum = s->spectrum;
     for (int k = 0; k < 3; ++k) { S.pos[k] = s->pos[k]; S.dir[k] = s->dir[k] / nrm; }
     S.xmin = s->xmin; S.xmax = s->xmax; S.ymin = s->ymin; S.ymax = s->ymax;
     S.energy = s->energy;
+    edges.clear(); wi.clear(); bin.clear();
     if (s->spectrum == 0) {
-        if (!(s->energy > 0)) { h->err = "source energy must be positive"; return EGSGPU_ERR_ARG; }
-    } else {
-        int nb = s->nbins;
-        if (nb < 1 || !s->edges || !s->weights) { h->err = "bad spectrum"; return EGSGPU_ERR_ARG; }
-        // Walker alias table over histogram bins (egs++/egs_alias_table.cpp:117-263)
-        std::vector<double> w(nb), wi(nb, 1.0);
-        std::vector<int> bin(nb, 0);
-        double sum = 0;
-        for (int i = 0; i < nb; ++i) {
-            if (!(s->edges[i + 1] > s->edges[i]) || s->weights[i] < 0) { h->err = "bad spectrum bins"; return EGSGPU_ERR_ARG; }
-            w[i] = s->weights[i] * (s->edges[i + 1] - s->edges[i]);
-            sum += w[i];
-        }
-        if (!(sum > 0)) { h->err = "empty spectrum"; return EGSGPU_ERR_ARG; }
-        for (int i = 0; i < nb; ++i) w[i] = w[i] / sum * nb;
-        std::vector<int> small, large;
-        for (int i = 0; i < nb; ++i) (w[i] < 1 ? small : large).push_back(i);
-        while (!small.empty() && !large.empty()) {
-            int sm = small.back(); small.pop_back();
-            int lg = large.back();
-            wi[sm] = w[sm]; bin[sm] = lg;
-            w[lg] -= 1 - w[sm];
-            if (w[lg] < 1) { large.pop_back(); small.push_back(lg); }
-        }
-        for (int i : small) { wi[i] = 1; bin[i] = i; }
-        for (int i : large) { wi[i] = 1; bin[i] = i; }
+        if (!(s->energy > 0)) { err = "source energy must be positive"; return EGSGPU_ERR_ARG; }
+        return 0;
+    }
+    int nb = s->nbins;
+    if (nb < 1 || !s->edges || !s->weights) { err = "bad spectrum"; return EGSGPU_ERR_ARG; }
+    std::vector<double> w(nb);
+    wi.assign(nb, 1.0);
+    bin.assign(nb, 0);
+    double sum = 0;
+    for (int i = 0; i < nb; ++i) {
+        if (!(s->edges[i + 1] > s->edges[i]) || s->weights[i] < 0) { err = "bad spectrum bins"; return EGSGPU_ERR_ARG; }
+        w[i] = s->weights[i] * (s->edges[i + 1] - s->edges[i]);
+        sum += w[i];
+    }
+    if (!(sum > 0)) { err = "empty spectrum"; return EGSGPU_ERR_ARG; }
+    for (int i = 0; i < nb; ++i) w[i] = w[i] / sum * nb;
+    std::vector<int> small, large;
+    for (int i = 0; i < nb; ++i) (w[i] < 1 ? small : large).push_back(i);
+    while (!small.empty() && !large.empty()) {
+        int sm = small.back(); small.pop_back();
+        int lg = large.back();
+        wi[sm] = w[sm]; bin[sm] = lg;
+        w[lg] -= 1 - w[sm];
+        if (w[lg] < 1) { large.pop_back(); small.push_back(lg); }
+    }
+    for (int i : small) { wi[i] = 1; bin[i] = i; }
+    for (int i : large) { wi[i] = 1; bin[i] = i; }
+    edges.assign(s->edges, s->edges + nb + 1);
+    S.nbins = nb;
+    return 0;
+}
+
+extern "C" {
+
+int egsgpu_set_source(egsgpu_handle *h, const egsgpu_source *s) {
+    if (!h || !s) return EGSGPU_ERR_ARG;
+    Source S;
+    std::vector<double> edges, wi;
+    std::vector<int> bin;
+    if (int rc = build_source(s, S, edges, wi, bin, h->err)) return rc;
+    if (s->shape == 2) {
         std::string &err = h->err;
+        CK(h->d_phsp.alloc((size_t)s->nphsp * 7 * sizeof(float)));
+        CK(cudaMemcpy(h->d_phsp.p, s->phsp, (size_t)s->nphsp * 7 * sizeof(float), cudaMemcpyHostToDevice));
+        S.phsp = (const float *)h->d_phsp.p;
+    } else if (s->spectrum == 1) {
+        std::string &err = h->err;
+        int nb = S.nbins;
         CK(h->d_edges.alloc((nb + 1) * sizeof(double)));
         CK(h->d_wi.alloc(nb * sizeof(double)));
         CK(h->d_bin.alloc(nb * sizeof(int)));
-        CK(cudaMemcpy(h->d_edges.p, s->edges, (nb + 1) * sizeof(double), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(h->d_edges.p, edges.data(), (nb + 1) * sizeof(double), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(h->d_wi.p, wi.data(), nb * sizeof(double), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(h->d_bin.p, bin.data(), nb * sizeof(int), cudaMemcpyHostToDevice));
-        S.nbins = nb;
         S.edges = (const double *)h->d_edges.p; S.wi = (const double *)h->d_wi.p; S.bin = (const int *)h->d_bin.p;
     }
     h->S = S;
@@ -1822,12 +2245,163 @@ int egsgpu_run(egsgpu_handle *h, long long first, long long n, int n_batch, uint
     return 0;
 }
 
+int egsgpu_set_phantoms(egsgpu_handle *h, int n, const egsgpu_phantom *ph) {
+    if (!h || n < 1 || !ph) return EGSGPU_ERR_ARG;
+    if (!h->have_media) { h->err = "load media before the phantoms"; return EGSGPU_ERR_STATE; }
+    const int nmed = (int)h->H.media.size();
+    std::vector<PhantomDesc> pd(n);
+    std::vector<Source> src(n);
+    std::vector<double> alle, allw;
+    std::vector<int> allb;
+    std::vector<long long> so(n, -1), bo(n, -1), po(n, -1);
+    long long nphsp_all = 0;
+    Source smax{};
+    long long tot = 0;
+    for (int k = 0; k < n; ++k) {
+        const egsgpu_phantom &q = ph[k];
+        const std::string at = " (phantom " + std::to_string(k) + ")";
+        if (q.nx < 1 || q.ny < 1 || q.nz < 1 || !q.xb || !q.yb || !q.zb || !q.med || !q.rhor) {
+            h->err = "bad phantom geometry" + at;
+            return EGSGPU_ERR_ARG;
+        }
+        if (q.histories < 0 || q.histories > 0xffffffffLL) { h->err = "bad history count" + at; return EGSGPU_ERR_ARG; }
+        long long nv = (long long)q.nx * q.ny * q.nz;
+        if (tot + nv > (1LL << 31) - 1) { h->err = "too many voxels over all phantoms"; return EGSGPU_ERR_ARG; }
+        tot += nv;
+        for (int i = 0; i < q.nx; ++i) if (!(q.xb[i + 1] > q.xb[i])) { h->err = "x-planes not increasing" + at; return EGSGPU_ERR_ARG; }
+        for (int i = 0; i < q.ny; ++i) if (!(q.yb[i + 1] > q.yb[i])) { h->err = "y-planes not increasing" + at; return EGSGPU_ERR_ARG; }
+        for (int i = 0; i < q.nz; ++i) if (!(q.zb[i + 1] > q.zb[i])) { h->err = "z-planes not increasing" + at; return EGSGPU_ERR_ARG; }
+        for (long long i = 0; i < nv; ++i) {
+            if (q.med[i] < 0 || q.med[i] >= nmed) { h->err = "voxel medium index out of range" + at; return EGSGPU_ERR_ARG; }
+            if (!(q.rhor[i] > 0) || !std::isfinite(q.rhor[i])) { h->err = "bad voxel relative density" + at; return EGSGPU_ERR_ARG; }
+        }
+        std::vector<double> e, w;
+        std::vector<int> b;
+        if (int rc = build_source(&q.source, src[k], e, w, b, h->err)) { h->err += at; return rc; }
+        double emax = q.source.energy;
+        if (q.source.shape == 2) {
+            po[k] = nphsp_all;
+            nphsp_all += q.source.nphsp;
+            emax = src[k].energy;
+        } else if (q.source.spectrum == 1) {
+            so[k] = (long long)allw.size();
+            bo[k] = (long long)alle.size();
+            alle.insert(alle.end(), e.begin(), e.end());
+            allw.insert(allw.end(), w.begin(), w.end());
+            allb.insert(allb.end(), b.begin(), b.end());
+            emax = e.back();
+        }
+        smax.energy = std::max(smax.energy, emax);
+        if (src[k].charge != 0) smax.charge = -1;
+        pd[k] = PhantomDesc{q.nx, q.ny, q.nz, q.xb, q.yb, q.zb, q.med, q.rhor, q.seed, q.histories};
+    }
+    std::string &err = h->err;
+    if (nphsp_all > 0) {
+        CK(h->d_pphsp.alloc((size_t)nphsp_all * 7 * sizeof(float)));
+        for (int k = 0; k < n; ++k) {
+            if (po[k] < 0) continue;
+            CK(cudaMemcpy((float *)h->d_pphsp.p + 7 * po[k], ph[k].source.phsp,
+                          (size_t)ph[k].source.nphsp * 7 * sizeof(float), cudaMemcpyHostToDevice));
+            src[k].phsp = (const float *)h->d_pphsp.p + 7 * po[k];
+        }
+    }
+    if (!allw.empty()) {
+        CK(h->d_pedges.alloc(alle.size() * sizeof(double)));
+        CK(h->d_pwi.alloc(allw.size() * sizeof(double)));
+        CK(h->d_pbin.alloc(allb.size() * sizeof(int)));
+        CK(cudaMemcpy(h->d_pedges.p, alle.data(), alle.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(h->d_pwi.p, allw.data(), allw.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(h->d_pbin.p, allb.data(), allb.size() * sizeof(int), cudaMemcpyHostToDevice));
+        for (int k = 0; k < n; ++k) {
+            if (so[k] < 0) continue;
+            src[k].edges = (const double *)h->d_pedges.p + bo[k];
+            src[k].wi = (const double *)h->d_pwi.p + so[k];
+            src[k].bin = (const int *)h->d_pbin.p + so[k];
+        }
+    }
+    int rc = h->eng->problems(n, pd.data(), src.data(), h->err);
+    if (rc) { h->phantoms.clear(); h->have_geom = false; return rc; }
+    h->phantoms.assign(n, egsgpu_handle::Phantom{});
+    long long voff = 0;
+    for (int k = 0; k < n; ++k) {
+        const egsgpu_phantom &q = ph[k];
+        egsgpu_handle::Phantom &P = h->phantoms[k];
+        long long nv = (long long)q.nx * q.ny * q.nz;
+        P.nx = q.nx; P.ny = q.ny; P.nz = q.nz;
+        P.xb.assign(q.xb, q.xb + q.nx + 1); P.yb.assign(q.yb, q.yb + q.ny + 1); P.zb.assign(q.zb, q.zb + q.nz + 1);
+        P.med.assign(q.med, q.med + nv); P.rhor.assign(q.rhor, q.rhor + nv);
+        P.voff = voff; P.histories = q.histories; P.nhist = 0;
+        voff += nv;
+    }
+    h->mvox = voff;
+    h->Smax = smax;
+    h->have_geom = true;
+    h->have_source = true;
+    h->nhist = 0; h->nbatch = 0;
+    return 0;
+}
+
+int egsgpu_run_phantoms(egsgpu_handle *h, int n_batch, void *stream) {
+    if (!h || n_batch < 1) return EGSGPU_ERR_ARG;
+    if (!h->multi()) { h->err = "no phantoms set"; return EGSGPU_ERR_STATE; }
+    for (auto &P : h->phantoms)
+        if (P.histories > 0 && P.histories < n_batch) { h->err = "a phantom has fewer histories than batches"; return EGSGPU_ERR_ARG; }
+    int rc = h->eng->run_multi(h->Smax, n_batch, (cudaStream_t)stream, h->err);
+    if (rc) return rc;
+    for (auto &P : h->phantoms) { P.nhist += P.histories; h->nhist += P.histories; }
+    h->nbatch += n_batch;
+    return 0;
+}
+
+int egsgpu_get_phantom_info(egsgpu_handle *h, int k, long long *out) {
+    if (!h || !out || k < 0 || k >= (int)h->phantoms.size()) return EGSGPU_ERR_ARG;
+    const auto &P = h->phantoms[k];
+    out[0] = P.voff; out[1] = (long long)P.nx * P.ny * P.nz; out[2] = P.nhist;
+    return 0;
+}
+
+}  // extern "C"
+
+template <class E>
+static int read_range_impl(egsgpu_handle *h, E *eng, long long off, long long n, double *sum, double *sum2) {
+    std::string &err = h->err;
+    if (sum) CK(cudaMemcpy(sum, (double *)eng->d_sum.p + off, n * sizeof(double), cudaMemcpyDeviceToHost));
+    if (sum2) CK(cudaMemcpy(sum2, (double *)eng->d_sum2.p + off, n * sizeof(double), cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+extern "C" {
+
+int egsgpu_get_phantom_dose(egsgpu_handle *h, int k, double *dose, double *sigma) {
+    if (!h || !dose || k < 0 || k >= (int)h->phantoms.size()) return EGSGPU_ERR_ARG;
+    const auto &P = h->phantoms[k];
+    long long nv = (long long)P.nx * P.ny * P.nz;
+    std::vector<double> s(nv), s2(nv);
+    int rc = h->cfg.precision == 32 ? read_range_impl(h, (Engine<float> *)h->eng.get(), P.voff, nv, s.data(), s2.data())
+                                    : read_range_impl(h, (Engine<double> *)h->eng.get(), P.voff, nv, s.data(), s2.data());
+    if (rc) return rc;
+    const double N = (double)P.nhist, nb = (double)h->nbatch;
+    for (long long i = 0; i < nv; ++i) {
+        int iz = (int)(i / ((long long)P.nx * P.ny)), rr = (int)(i - (long long)iz * P.nx * P.ny);
+        int iy = rr / P.nx, ix = rr - iy * P.nx;
+        double vol = (P.xb[ix + 1] - P.xb[ix]) * (P.yb[iy + 1] - P.yb[iy]) * (P.zb[iz + 1] - P.zb[iz]);
+        double mass = vol * P.rhor[i] * h->H.media[P.med[i]].rho;
+        double norm = N > 0 ? 1.602e-10 / (mass * N) : 0;   // egs_dose_scoring.cpp:318-319
+        dose[i] = s[i] * norm;
+        if (sigma) {
+            double mean = s[i] / nb, var = nb > 1 ? (s2[i] / nb - mean * mean) / (nb - 1) : 0;
+            sigma[i] = (var > 0 ? std::sqrt(var) * nb : 0) * norm;
+        }
+    }
+    return 0;
+}
+
 int egsgpu_reset(egsgpu_handle *h) {
     if (!h || !h->have_geom) return EGSGPU_ERR_STATE;
     std::string &err = h->err;
     EngineBase *e = h->eng.get();
     (void)e;
-    long long nv = (long long)h->nx * h->ny * h->nz;
+    long long nv = h->nvox();
     auto reset = [&](auto *eng) -> int {
         CK(cudaMemset(eng->d_dose.p, 0, nv * sizeof(double)));
         CK(cudaMemset(eng->d_sum.p, 0, nv * sizeof(double)));
@@ -1841,6 +2415,7 @@ int egsgpu_reset(egsgpu_handle *h) {
     int rc = h->cfg.precision == 32 ? reset((Engine<float> *)h->eng.get()) : reset((Engine<double> *)h->eng.get());
     if (rc) return rc;
     h->nhist = 0; h->nbatch = 0;
+    for (auto &P : h->phantoms) P.nhist = 0;
     return 0;
 }
 
@@ -1872,7 +2447,8 @@ int egsgpu_get_tallies(egsgpu_handle *h, double *sum, double *sum2, double *tota
 
 int egsgpu_get_dose(egsgpu_handle *h, double *dose, double *sigma) {
     if (!h || !h->have_geom || !dose) return EGSGPU_ERR_ARG;
-    long long nv = (long long)h->nx * h->ny * h->nz;
+    if (h->multi()) { h->err = "several phantoms are set: use egsgpu_get_phantom_dose"; return EGSGPU_ERR_STATE; }
+    long long nv = h->nvox();
     std::vector<double> s(nv), s2(nv);
     int rc = egsgpu_get_tallies(h, s.data(), s2.data(), nullptr);
     if (rc) return rc;
@@ -1890,6 +2466,33 @@ int egsgpu_get_dose(egsgpu_handle *h, double *dose, double *sigma) {
             sigma[i] = (var > 0 ? std::sqrt(var) * nb : 0) * norm;
         }
     }
+    return 0;
+}
+
+int egsgpu_adjoint(egsgpu_handle *h, long long first, long long n, uint32_t seed, const double *dL_dD,
+                   double *dL_drhor) {
+    if (!h || !dL_dD || !dL_drhor || n < 1 || first < 0 || first + n > 0xffffffffLL) return EGSGPU_ERR_ARG;
+    if (!h->have_media || !h->have_geom || !h->have_source || h->multi()) {
+        h->err = "media, one geometry and a source must be set";
+        return EGSGPU_ERR_STATE;
+    }
+    if (h->nhist != n) { h->err = "the tallies must hold exactly the n histories being differentiated"; return EGSGPU_ERR_STATE; }
+    long long nv = h->nvox();
+    std::vector<double> s(nv), w(nv), D(nv);
+    int rc = egsgpu_get_tallies(h, s.data(), nullptr, nullptr);
+    if (rc) return rc;
+    for (long long i = 0; i < nv; ++i) {
+        int iz = (int)(i / ((long long)h->nx * h->ny)), rr = (int)(i - (long long)iz * h->nx * h->ny);
+        int iy = rr / h->nx, ix = rr - iy * h->nx;
+        double vol = (h->xb[ix + 1] - h->xb[ix]) * (h->yb[iy + 1] - h->yb[iy]) * (h->zb[iz + 1] - h->zb[iz]);
+        double norm = 1.602e-10 / (vol * h->rhor[i] * h->H.media[h->med[i]].rho * (double)n);
+        D[i] = s[i] * norm;
+        w[i] = dL_dD[i] * norm;   // dL/dE_v
+    }
+    rc = h->eng->adjoint(h->S, first, n, seed, w.data(), dL_drhor, h->err);
+    if (rc) return rc;
+    // D = E / (rho V): the explicit dependence on the voxel's own density
+    for (long long i = 0; i < nv; ++i) dL_drhor[i] -= dL_dD[i] * D[i] / h->rhor[i];
     return 0;
 }
 
@@ -1921,7 +2524,7 @@ int egsgpu_get_history_tally(egsgpu_handle *h, double *out) {
 // Checkpoint layout: magic, nvox, nhist, nbatch, energy[2], counters[8], sum[nvox], sum2[nvox]
 int egsgpu_checkpoint(egsgpu_handle *h, void *buf, size_t *size) {
     if (!h || !size || !h->have_geom) return EGSGPU_ERR_ARG;
-    long long nv = (long long)h->nx * h->ny * h->nz;
+    long long nv = h->nvox();
     size_t need = 8 * 4 + 2 * 8 + 8 * 8 + 2 * nv * 8;
     if (!buf) { *size = need; return 0; }
     if (*size < need) { *size = need; h->err = "checkpoint buffer too small"; return EGSGPU_ERR_ARG; }
@@ -1942,7 +2545,7 @@ int egsgpu_checkpoint(egsgpu_handle *h, void *buf, size_t *size) {
 
 int egsgpu_restore(egsgpu_handle *h, const void *buf, size_t size) {
     if (!h || !buf || !h->have_geom) return EGSGPU_ERR_ARG;
-    long long nv = (long long)h->nx * h->ny * h->nz;
+    long long nv = h->nvox();
     size_t need = 8 * 4 + 2 * 8 + 8 * 8 + 2 * nv * 8;
     const char *b = (const char *)buf;
     long long hdr[4];

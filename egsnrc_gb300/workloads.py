@@ -10,12 +10,19 @@
                ECUT 0.521 MeV (2e8 histories, seed 3)
   perturbed64  64^3 x 0.3 cm water with relative densities 1 + 0.1 u,
                u ~ U(-1,1) (seed 11), 6 MeV photon 5x5 cm field (seed 13)
+  batched64    64 independent problems run together: cubes of n ~ U{32..160}
+               voxels of 0.2 cm whose densities are a Gaussian random field
+               (1 cm smoothing) mapped to 0.2-1.9 g/cc and to four media by
+               threshold; per problem a photon or electron 10 cm-deep parallel
+               beam of E ~ U(1, 18) MeV and a square field of side ~ U(2, 15) cm;
+               histories log-uniform on [1e6, 5e7]; problem k draws from seed
+               1000 + k and transports with Philox seed 2000 + k
 The phantom occupies x, y in [-L/2, L/2] and z in [0, L]; beams start at
 z = -1 cm travelling along +z.
 """
 import numpy as np
 
-from . import ParallelBeam, XYZGeometry
+from . import PEGS_FILE, ParallelBeam, XYZGeometry
 
 WATER = "H2O521ICRU"
 LUNG = "LUNG521ICRU"
@@ -69,6 +76,56 @@ def perturbed64(n=64, seed=11):
                 source=ParallelBeam(charge=0, energy=6.0, position=(0.0, 0.0, -1.0),
                                     rectangle=(-2.5, 2.5, -2.5, 2.5)),
                 histories=int(2e7), batches=10, seed=13)
+
+
+def pegs_density(name, path=PEGS_FILE):
+    """Mass density (g/cm^3) of a medium as written in its PEGS4 block."""
+    key = " MEDIUM=" + name
+    with open(path) as f:
+        for line in f:
+            if line.startswith(key) and line[8:32].strip() == name:
+                comp = next(f)
+                return float(comp.split("RHO=")[1].split(",")[0])
+    raise KeyError(name)
+
+
+def gaussian_field(n, sigma_vox, rng):
+    """Zero-mean white noise on an n^3 grid smoothed by a Gaussian of
+    `sigma_vox` voxels (periodic, through the FFT)."""
+    k = np.fft.fftfreq(n)
+    kz, ky, kx = np.meshgrid(k, k, np.fft.rfftfreq(n), indexing="ij")
+    filt = np.exp(-2.0 * (np.pi * sigma_vox) ** 2 * (kx * kx + ky * ky + kz * kz))
+    return np.fft.irfftn(np.fft.rfftn(rng.standard_normal((n, n, n))) * filt, s=(n, n, n), axes=(0, 1, 2))
+
+
+BATCH_MEDIA = [LUNG, WATER, TISSUE, BONE]
+BATCH_THRESHOLDS = [0.6, 1.05, 1.4]     # g/cc boundaries between the media above
+
+
+def batch_problem(k, edge=(32, 160), dx=0.2, hist=(1e6, 5e7), scale=1.0, seed0=1000, philox0=2000):
+    """Problem k of the batched workload (see the module docstring)."""
+    rng = np.random.default_rng(seed0 + k)
+    n = int(rng.integers(edge[0], edge[1] + 1))
+    charge = 0 if rng.uniform() < 0.5 else -1
+    energy = float(rng.uniform(1.0, 18.0))
+    side = float(rng.uniform(2.0, 15.0))
+    nh = float(np.exp(rng.uniform(np.log(hist[0]), np.log(hist[1]))))
+    f = gaussian_field(n, 1.0 / dx, rng)
+    rho = 0.2 + 1.7 * (f - f.min()) / max(f.max() - f.min(), 1e-30)
+    med = np.searchsorted(BATCH_THRESHOLDS, rho, side="right").astype(np.int32)
+    dens = np.array([pegs_density(m) for m in BATCH_MEDIA])
+    rhor = rho / dens[med]
+    h = side / 2
+    return dict(geometry=centred_geometry(n, dx, med.ravel(), rhor.ravel()),
+                source=ParallelBeam(charge=charge, energy=energy, position=(0.0, 0.0, -1.0),
+                                    rectangle=(-h, h, -h, h)),
+                seed=philox0 + k, histories=max(1, int(round(nh * scale))), edge=n, rho=rho.ravel())
+
+
+def batched64(nprob=64, scale=1.0, edge=(32, 160)):
+    """The batched workload; `scale` multiplies every problem's histories."""
+    return dict(name="batched64", media=BATCH_MEDIA, ecut=0.7, pcut=0.01,
+                problems=[batch_problem(k, edge=edge, scale=scale) for k in range(nprob)], batches=10)
 
 
 WORKLOADS = {"water30": water30, "slab64": slab64, "water128e": water128e, "perturbed64": perturbed64}

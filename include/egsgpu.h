@@ -58,7 +58,9 @@ typedef struct {
 
 /* Source: egs++ EGS_ParallelBeam (sources/egs_parallel_beam) with a point
  * or rectangle shape (shapes/egs_rectangle) and a monoenergetic or
- * histogram spectrum (egs_spectra.cpp:491-740). */
+ * histogram spectrum (egs_spectra.cpp:491-740), or (shape 2) a phase-space
+ * source: egs++ EGS_PhspSource / DOSXYZnrc isource 2
+ * (sources/egs_phsp_source/egs_phsp_source.cpp:284-440). */
 typedef struct {
     int charge;           /* -1 e-, 0 photon, +1 e+                          */
     int shape;            /* 0 point, 1 rectangle in the plane z = pos[2]    */
@@ -70,6 +72,15 @@ typedef struct {
     int nbins;            /* spectrum 1: number of bins                       */
     const double *edges;  /* spectrum 1: nbins+1 bin edges (MeV)              */
     const double *weights;/* spectrum 1: nbins values, counts per MeV         */
+    /* shape 2: nphsp particles of 7 floats {charge, kinetic energy (MeV),
+     * x, y, u, v, weight}, as in an .egsphsp file: a negative weight means a
+     * negative w.  Particle i starts at (x + pos[0], y + pos[1], pos[2]) with
+     * direction (u, v, +-sqrt(1 - u^2 - v^2)); history h uses particle
+     * (h / (recycle + 1)) mod nphsp with weight |weight| / (recycle + 1).
+     * dir, spectrum and energy are ignored. */
+    long long nphsp;
+    const float *phsp;
+    int recycle;
 } egsgpu_source;
 
 /* Default configuration (the egs_set_defaults profile, FP32 transport). */
@@ -130,6 +141,57 @@ int egsgpu_get_tallies(egsgpu_handle *h, double *edep_sum, double *edep2_sum, do
  * EGS_DoseScoring::reportResults/outputDoseFile
  * (ausgab_objects/egs_dose_scoring/egs_dose_scoring.cpp:309-480). */
 int egsgpu_get_dose(egsgpu_handle *h, double *dose, double *sigma);
+
+/* Several independent dose problems transported together.  The reference
+ * runs one problem per process (an egs++ application with one geometry and
+ * one source, egs++/egs_application.cpp:839-959; parallel jobs are separate
+ * processes combined afterwards, egs_application.cpp:624).  Here every
+ * phantom keeps its own geometry, source, Philox seed and history count, and
+ * all phantoms share each wavefront, so small problems fill the GPU together.
+ * Phantom k's results equal those of runs of its own with the same seed,
+ * history ranges and batch count. */
+typedef struct {
+    int nx, ny, nz;
+    const double *xb, *yb, *zb;     /* nx+1, ny+1, nz+1 plane positions (cm) */
+    const int32_t *med;             /* medium index per voxel (x fastest)   */
+    const double *rhor;             /* relative density per voxel           */
+    egsgpu_source source;
+    uint32_t seed;                  /* Philox seed of this phantom          */
+    long long histories;            /* histories per egsgpu_run_phantoms   */
+} egsgpu_phantom;
+
+/* Replaces the single geometry and source by n phantoms (host arrays are
+ * copied).  Until the next egsgpu_set_xyz_geometry, egsgpu_run and
+ * egsgpu_get_dose return EGSGPU_ERR_STATE, and egsgpu_get_tallies returns
+ * the phantoms' voxels laid end to end (offsets from egsgpu_get_phantom_info). */
+int egsgpu_set_phantoms(egsgpu_handle *h, int n, const egsgpu_phantom *phantoms);
+/* Transports every phantom's next `histories` histories in n_batch batches,
+ * all phantoms in the same wavefronts (each batch: the same history split as
+ * egsgpu_run).  The first call runs histories [0, n_k) of phantom k, the
+ * second [n_k, 2 n_k), and so on. */
+int egsgpu_run_phantoms(egsgpu_handle *h, int n_batch, void *stream);
+/* Dose (Gy per source particle) and 1-sigma of phantom k. */
+int egsgpu_get_phantom_dose(egsgpu_handle *h, int k, double *dose, double *sigma);
+/* out[3] = {first global voxel index, voxels, histories run so far} of phantom k. */
+int egsgpu_get_phantom_info(egsgpu_handle *h, int k, long long *out);
+
+/* Gradient of a loss of the dose with respect to the voxels' relative
+ * densities (rhor; the mass density is rhor times the medium's PEGS4
+ * density).  The handle's tallies must hold exactly the run being
+ * differentiated: histories [first, first+n) with `seed`, since the last
+ * reset.  dL_dD[nvox] is the loss's derivative with respect to that run's dose
+ * (Gy per particle, as from egsgpu_get_dose); dL_drhor[nvox] receives
+ * dL/d(rhor).  The histories are replayed from their seeds twice (no paths
+ * are stored): first to weigh each history's deposits by dL/dE, then with
+ * adjoint kernels that add the photon path scores (attenuation and
+ * interaction likelihoods scale with rhor) and the pathwise term of the
+ * electrons' continuous energy loss; the dose's explicit 1/rhor factor is
+ * added on the host.  No counterpart in the reference (which has no
+ * derivatives); the density scaling it differentiates is the reference's
+ * RHOF (src/egsnrc.mortran PHOTON GMFP = GMFPR0/RHOF, ELECTR tstep/rhof,
+ * interface/egs_c_interface2.macros:398). */
+int egsgpu_adjoint(egsgpu_handle *h, long long first, long long n, uint32_t seed, const double *dL_dD,
+                   double *dL_drhor);
 
 /* Optional per-history deposited energy (MeV) for histories
  * [first, first+n) of the next egsgpu_run call (n <= 2^24); pass NULL to

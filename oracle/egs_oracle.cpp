@@ -144,6 +144,7 @@ struct Source {
     // alias table (egs_alias_table.cpp:117-263 layout: wi, bin)
     std::vector<double> wi;
     std::vector<int> bin;
+    std::vector<float> phsp;           // phase-space particles (7 floats each)
 };
 
 struct Tally {
@@ -1340,12 +1341,27 @@ bool source_particle(Run &R, uint32_t hist, Particle &p) {
     p = Particle();
     p.hist = hist; p.sid = 0; p.n = 0; p.cache_blk = -1; p.wt = 1;
     double x = S.s.pos[0], y = S.s.pos[1], z = S.s.pos[2];
+    double u = S.s.dir[0], v = S.s.dir[1], w = S.s.dir[2];
+    int charge = S.s.charge;
     if (S.s.shape == 1) {
         x = S.s.xmin + (S.s.xmax - S.s.xmin) * rnd(R, p);
         y = S.s.ymin + (S.s.ymax - S.s.ymin) * rnd(R, p);
     }
     double ek;
-    if (S.s.spectrum == 0) ek = S.s.energy;
+    if (S.s.shape == 2) {
+        // EGS_PhspSource::getNextParticle (egs++/sources/egs_phsp_source/egs_phsp_source.cpp:284-323):
+        // position in the source plane, w from u and v with the sign of the
+        // weight; each particle used recycle + 1 times with its weight shared
+        const float *q = S.phsp.data() + 7 * (((long long)hist / (S.s.recycle + 1)) % S.s.nphsp);
+        charge = (int)q[0];
+        ek = q[1];
+        x += q[2]; y += q[3];
+        u = q[4]; v = q[5];
+        double a = u * u + v * v;
+        w = a < 1 ? std::sqrt(1 - a) : 0.0;
+        if (q[6] < 0) w = -w;
+        p.wt = std::fabs((double)q[6]) / (S.s.recycle + 1);
+    } else if (S.s.spectrum == 0) ek = S.s.energy;
     else {
         int np = S.s.nbins;
         double aj = rnd(R, p) * np;
@@ -1354,10 +1370,10 @@ bool source_particle(Run &R, uint32_t hist, Particle &p) {
         if (aj > S.wi[j]) j = S.bin[j];
         ek = S.edges[j] + (S.edges[j + 1] - S.edges[j]) * rnd(R, p);
     }
-    p.iq = S.s.charge;
+    p.iq = charge;
     p.E = (p.iq == 0) ? ek : ek + RM;
     p.x = x; p.y = y; p.z = z;
-    p.u = S.s.dir[0]; p.v = S.s.dir[1]; p.w = S.s.dir[2];
+    p.u = u; p.v = v; p.w = w;
     int ir = is_where(R.O->G, x, y, z);
     if (ir < 0) {
         double t = 1e10;
@@ -1442,7 +1458,11 @@ int oracle_set_source(oracle_handle *h, const egsgpu_source *s) {
     h->O.S.s = *s;
     double n = std::sqrt(s->dir[0] * s->dir[0] + s->dir[1] * s->dir[1] + s->dir[2] * s->dir[2]);
     for (int k = 0; k < 3; ++k) h->O.S.s.dir[k] = s->dir[k] / n;
-    if (s->spectrum == 1) build_alias(h->O.S);
+    if (s->shape == 2) {
+        if (s->nphsp < 1 || !s->phsp || s->recycle < 0) return 1;
+        h->O.S.phsp.assign(s->phsp, s->phsp + 7 * s->nphsp);
+        h->O.S.s.phsp = nullptr;
+    } else if (s->spectrum == 1) build_alias(h->O.S);
     return 0;
 }
 

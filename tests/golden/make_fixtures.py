@@ -2,6 +2,10 @@
 
   ndgeom_egsphant.egsphant.gz  egs++/geometry/examples/ndgeom_egsphant.egsphant
                                (the reference's example voxel phantom), gzipped
+  EXslabs.egsphsp1.gz          omega/beamnrc/BEAMnrc_examples/EXslabs/EXslabs.egsphsp1
+  EX16MVp.egsphsp1.gz          omega/beamnrc/BEAMnrc_examples/EX16MVp/EX16MVp.egsphsp1
+                               (BEAMnrc example phase-space files, MODE0 and
+                               MODE2, shipped with the reference), gzipped
 
 Usage: python tests/golden/make_fixtures.py <HEN_HOUSE>
 """
@@ -17,3 +21,7 @@ if __name__ == "__main__":
     src = os.path.join(hh, "egs++", "geometry", "examples", "ndgeom_egsphant.egsphant")
     with open(src, "rb") as f, gzip.open(os.path.join(HERE, "ndgeom_egsphant.egsphant.gz"), "wb", 9) as g:
         shutil.copyfileobj(f, g)
+    for name in ("EXslabs", "EX16MVp"):
+        src = os.path.join(hh, "omega", "beamnrc", "BEAMnrc_examples", name, name + ".egsphsp1")
+        with open(src, "rb") as f, gzip.open(os.path.join(HERE, name + ".egsphsp1.gz"), "wb", 9) as g:
+            shutil.copyfileobj(f, g)

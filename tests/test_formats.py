@@ -49,3 +49,38 @@ def test_3ddose_roundtrip(tmp_path):
     assert (nx, ny, nz) == (6, 6, 6)
     assert np.allclose(d2, d.astype(np.float32), rtol=1e-6)
     assert r2[3] == 1.0 and np.allclose(r2[d > 0], 0.01, rtol=1e-5)
+
+
+def test_reference_phase_space_files_are_self_consistent():
+    # BEAMnrc example phase-space files shipped with the reference (MODE0 and
+    # MODE2): the records reproduce the counts and energies of their header
+    for name, mode, n, nphot, ninc in (("EXslabs", "MODE0", 1030, 31, 1000.0),
+                                       ("EX16MVp", "MODE2", 3882, 2542, 15000.0)):
+        p, h = formats.read_egsphsp(os.path.join(GOLDEN, name + ".egsphsp1.gz"))
+        assert (h["mode"], h["n"], h["photons"], h["incident"]) == (mode, n, nphot, ninc)
+        assert p.shape == (n, 7)
+        assert int((p[:, 0] == 0).sum()) == nphot
+        assert p[:, 1].max() == np.float32(h["ekmax"])
+        assert abs(p[p[:, 0] != 0, 1].min() - h["ekmin_e"]) < 2e-6
+        assert np.all(p[:, 1] > 0) and np.all(np.abs(p[:, 6]) > 0)
+        assert np.all(p[:, 4] ** 2 + p[:, 5] ** 2 <= 1 + 1e-5)
+        assert 0 < h["new_history"].sum() <= ninc
+
+
+def test_phase_space_roundtrip(tmp_path):
+    rng = np.random.default_rng(3)
+    k = 500
+    u = rng.uniform(-0.5, 0.5, k)
+    v = rng.uniform(-0.5, 0.5, k)
+    p = np.stack([rng.choice([-1, 0, 1], k), rng.uniform(0.1, 10, k), rng.uniform(-5, 5, k),
+                  rng.uniform(-5, 5, k), u, v, rng.choice([-1, 1], k) * rng.uniform(0.5, 2, k)], 1)
+    newh = rng.uniform(size=k) < 0.3
+    for mode in ("MODE0", "MODE2"):
+        f = str(tmp_path / ("t_" + mode + ".egsphsp1"))
+        formats.write_egsphsp(f, p, incident=123.0, new_history=newh, mode=mode)
+        q, h = formats.read_egsphsp(f)
+        assert h["mode"] == mode and h["n"] == k and h["incident"] == 123.0
+        assert np.array_equal(h["new_history"], newh)
+        assert np.array_equal(q[:, 0], p[:, 0])
+        assert np.allclose(q[:, 1], p[:, 1], rtol=1e-6, atol=2e-6)
+        assert np.allclose(q[:, 2:], p[:, 2:], rtol=1e-6, atol=1e-6)

@@ -42,3 +42,28 @@ def test_child_streams_are_distinct():
             for k in range(3):
                 seen.add(L.oracle_child_sid(sid, n, k))
     assert len(seen) == 3 * 64 * 3
+
+
+def test_oracle_phase_space_source_conserves_energy():
+    # every phase-space particle enters the phantom (field inside its face):
+    # deposited + escaped = sum of weight x (kinetic energy, + 2 m c^2 for e+)
+    import egsnrc_gb300 as eg
+    from egsnrc_gb300 import workloads as W
+    from oracle.oracle_binding import Oracle
+    rng = np.random.default_rng(8)
+    k = 64
+    p = np.stack([rng.choice([-1, 0, 1], k, p=[0.3, 0.6, 0.1]), rng.uniform(0.2, 4.0, k), rng.uniform(-2, 2, k),
+                  rng.uniform(-2, 2, k), rng.uniform(-0.2, 0.2, k), rng.uniform(-0.2, 0.2, k),
+                  rng.uniform(0.5, 1.5, k)], 1).astype(np.float32)
+    src = eg.PhaseSpaceSource(p, position=(0.0, 0.0, 0.0), recycle=1)
+    ora = Oracle([W.WATER], ecut=0.7, pcut=0.01)
+    ora.set_geometry(W.centred_geometry(12, 1.0))
+    ora.set_source(src)
+    n = 2 * k * 3
+    ora.run(n, nbatch=2, seed=4)
+    _, _, t = ora.tallies()    # totals: histories, batches, deposited, escaped, ...
+    e = 0.0
+    for h in range(n):
+        q = p[(h // 2) % k]
+        e += abs(float(q[6])) / 2 * (float(q[1]) + (2 * eg.RM if q[0] > 0 else 0.0))
+    assert abs(t[2] + t[3] - e) < 1e-9 * e

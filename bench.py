@@ -47,6 +47,11 @@ def parse():
     ap.add_argument("--chunk", type=int, default=0, help="histories per wavefront chunk (0 = automatic)")
     ap.add_argument("--clock-period", type=float, default=0.2, help="seconds between clock samples")
     ap.add_argument("--clock-mode", default="nvml", choices=["nvml", "process", "off"])
+    ap.add_argument("--adjoint", action="store_true",
+                    help="also time the seed-replay gradient of sum (D - T)^2 over all voxel densities "
+                         "(T from a second density map; the perturbed64 workload is config c5)")
+    ap.add_argument("--howfarless", action="store_true",
+                    help="DOSXYZnrc HOWFARLESS transport (homogeneous phantoms: water30, water128e)")
     ap.add_argument("--scale", type=float, default=0.005,
                     help="batched64: fraction of each phantom's 1e6-5e7 histories run per step")
     return ap.parse_args()
@@ -262,9 +267,10 @@ def reference_arm(args, wl, ws, rank, dist):
     print(json.dumps(line), flush=True)
 
 
-def config_of(wl, per_step):
+def config_of(wl, per_step, howfarless=False):
     g = wl["geometry"]
-    return {"workload": wl["name"], "phantom": "%dx%dx%d voxels" % (g.nx, g.ny, g.nz),
+    return {"workload": wl["name"] + ("-howfarless" if howfarless else ""),
+            "phantom": "%dx%dx%d voxels" % (g.nx, g.ny, g.nz),
             "media": wl["media"], "histories_per_step": int(per_step), "batches_per_step": 1,
             "ecut_MeV": wl["ecut"], "pcut_MeV": wl["pcut"],
             "l2": "256 MiB buffer written between timed steps"}
@@ -464,6 +470,33 @@ def bench_batched(args, ws, rank, local, dist):
         dist.destroy_process_group()
 
 
+def adjoint_leg(args, wl, eg, ekw, H):
+    """Forward run plus egsgpu_adjoint for L = sum (D - T)^2, T simulated on a
+    second density map (uniform +-10% perturbations from seed 12)."""
+    import torch
+    g = wl["geometry"]
+    rng = np.random.default_rng(12)
+    gt = eg.XYZGeometry(g.xb, g.yb, g.zb, g.med, 1.0 + 0.1 * rng.uniform(-1.0, 1.0, g.nvox))
+    e = eg.DoseEngine(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], precision=args.precision, **ekw)
+    e.set_source(wl["source"])
+    e.set_geometry(gt)
+    e.run(H, nbatch=10, seed=wl["seed"] + 1)
+    T, _ = e.dose()
+    e.set_geometry(g)
+    e.reset()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e.run(H, nbatch=10, seed=wl["seed"])
+    D, _ = e.dose()
+    t1 = time.perf_counter()
+    grad = e.adjoint(2 * (D - T), H, seed=wl["seed"])
+    t2 = time.perf_counter()
+    e.close()
+    return {"histories": int(H), "forward_s": t1 - t0, "adjoint_s": t2 - t1, "gradient_voxels": int(g.nvox),
+            "loss": float(((D - T) ** 2).sum()), "grad_abs_max": float(np.abs(grad).max()),
+            "path": "egsgpu_run + egsgpu_get_dose, then egsgpu_adjoint (two replays of the same histories)"}
+
+
 def main():
     args = parse()
     from egsnrc_gb300 import workloads as W
@@ -484,7 +517,7 @@ def main():
     torch.cuda.set_device(local)
     H = int(args.histories)
     K, Wm = args.steps, args.warmup
-    ekw = dict(capacity=args.capacity, chunk=args.chunk)
+    ekw = dict(capacity=args.capacity, chunk=args.chunk, howfarless=int(args.howfarless))
     eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], precision=args.precision, **ekw)
     eng.set_geometry(wl["geometry"])
     eng.set_source(wl["source"])
@@ -573,10 +606,12 @@ def main():
     line = {"metric": "histories_per_second", "value": value, "unit": "histories/s", "n_gpus": ws, "steps": K,
             "warmup": Wm, "ms_per_step": 1e3 * T / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32" if args.precision == 32 else "f64", "data": "synthetic",
-            "config": config_of(wl, H), "dose_efficiency": eff, "dose_efficiency_unit": "1/(sigma^2 s)",
+            "config": config_of(wl, H, args.howfarless), "dose_efficiency": eff, "dose_efficiency_unit": "1/(sigma^2 s)",
             "sigma_bar_50pct": sig, "voxels_above_50pct": nsel, "e2e": e2e, "roofline": roof,
             "gpu_launches": int(launches), "host_seconds": t_host}
 
+    if rank == 0 and args.adjoint:
+        line["adjoint"] = adjoint_leg(args, wl, eg, ekw, H)
     if rank == 0 and not args.no_fp64 and args.precision == 32:
         # plain FP64 GPU form on the same problem: histories/s and efficiency
         e64 = eg.DoseEngine(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], precision=64, **ekw)

@@ -32,7 +32,8 @@ class Config(C.Structure):
     _fields_ = [("ecut", C.c_double), ("pcut", C.c_double), ("estepe", C.c_double), ("ximax", C.c_double),
                 ("skindepth", C.c_double), ("precision", C.c_int), ("block_size", C.c_int),
                 ("ctas_per_sm", C.c_int), ("chunk", C.c_longlong), ("capacity", C.c_longlong),
-                ("requeue_lanes", C.c_int), ("use_graph", C.c_int), ("inter_batch", C.c_int)]
+                ("requeue_lanes", C.c_int), ("use_graph", C.c_int), ("inter_batch", C.c_int),
+                ("howfarless", C.c_int)]
 
 
 class SourceStruct(C.Structure):

@@ -64,7 +64,14 @@ struct Geom {
     const Real *rhor;
     Real bt, hbt;         // boundary tolerance (egs++/egs_functions.h:80-88)
     int voff;             // global index of this phantom's first voxel
+    // voxel-index decoding without integer division: n / nx and n / nxy as
+    // (umulhi(n, m) + n) >> l with m, l from fast_divisor (exact for n < 2^31)
+    uint32_t mnx, mnxy;
+    int lnx, lnxy;
 };
+__device__ inline int fdiv(int n, uint32_t m, int l) {
+    return (int)((__umulhi((uint32_t)n, m) + (uint32_t)n) >> l);
+}
 
 // ------------------------------------------------------------- source ----
 struct Source {

@@ -256,6 +256,32 @@ int read_pegs4(const std::string &path, const std::vector<std::string> &names,
 
 }  // namespace
 
+void howfarless_tmxs(const Medium &m, const TransportParams &p, double mindel, std::vector<double> &t0,
+                     std::vector<double> &t1) {
+    const int neke = m.meke;
+    t0.assign(neke, 0.0);
+    t1.assign(neke, 0.0);
+    // the estepe / ximax step length at energy e with stopping power dedx
+    auto step = [&](double e, double dedx) {
+        double p2 = e * (e + 2 * RM), beta2 = p2 / (p2 + RM * RM);
+        double chi_a2 = m.xcc / (4 * p2 * m.blcc);
+        double estepx = 2 * p2 * beta2 * dedx / e / m.xcc / (std::log(1 + 1. / chi_a2) * (1 + chi_a2) - 1);
+        estepx = std::min(estepx * p.ximax, p.estepe);
+        return std::max(estepx * e / dedx, mindel / 2);
+    };
+    double eil = (1 - m.eke0) / m.eke1;
+    double si = step(std::exp(eil), m.ededx1[0] * eil + m.ededx0[0]);
+    for (int i = 1; i <= neke - 1; ++i) {
+        double elke = (i + 1 - m.eke0) / m.eke1;
+        double sip1 = step(std::exp(elke), m.ededx1[i] * elke + m.ededx0[i]);
+        t1[i - 1] = (sip1 - si) * m.eke1;
+        t0[i - 1] = sip1 - t1[i - 1] * elke;
+        si = sip1;
+    }
+    t0[neke - 1] = t0[neke - 2];
+    t1[neke - 1] = t1[neke - 2];
+}
+
 double kn_sigma0(double e) {   // egs_KN_sigma0, egsnrc.mortran:8728-8745
     const double con = 0.1274783851;
     double ko = e / RM;

@@ -122,4 +122,12 @@ int hatch(const std::string &data_dir, const std::string &pegs_file,
 // Klein-Nishina total cross section per electron (egsnrc.mortran:8728-8745).
 double kn_sigma0(double e);
 
+// Largest condensed-history step for DOSXYZnrc's HOWFARLESS transport in a
+// homogeneous phantom (dosxyznrc.mortran modify_tmxs, :4795-4840): the
+// estepe / ximax step at every node of the electron energy grid, but never
+// below half the smallest voxel dimension `mindel` (cm).  Returns the
+// piecewise-linear coefficients (t0 + t1 * log E per bin) of medium m.
+void howfarless_tmxs(const Medium &m, const TransportParams &p, double mindel, std::vector<double> &t0,
+                     std::vector<double> &t1);
+
 }  // namespace egs

@@ -151,33 +151,52 @@ __device__ inline void gadd(const Params<Real> &P, AccG<Real> &a, int ir, Real g
     }
     a.g += g;
 }
-// Pathwise term of an electron's continuous energy loss.  With the random
-// numbers of a condensed-history step fixed in energy-loss units, the energy
-// lost inside voxel v scales with its density: d(de)/d(rhor_v) = de/rhor_v,
-// and the same energy is missing where the track ends (the voxel of its
-// cut-off deposit; nothing for a track that leaves the phantom or
-// annihilates).  ELIST voxel visits are kept per electron; a longer track is
-// closed early at its current voxel.
+// Pathwise derivative of an electron track's continuous energy loss (the
+// adjoint's electron term).  With a condensed-history step's random numbers
+// fixed in mass units, raising rhor_j shortens the track's path inside voxel
+// j, so every later voxel-face crossing moves along the track by
+// c_j[a] / (rhor_j u[a]) -- c_j the track's chord vector inside j so far, a
+// the axis of the crossed face, u the direction at the crossing -- and the
+// energy lost over that shift (dE/dx in the voxel being left) moves from the
+// voxel entered (weight w_b; 0 outside the phantom) to the one left (w_a).
+// Each visit to a voxel keeps its chord vector and accumulates
+// K = sum over later crossings of (w_a - w_b) dE/dx c[a] / u[a]; the track's
+// end adds K / rhor to dL/d(rhor) of the visited voxel.  ELIST visits are
+// kept per electron; a longer track flushes its oldest part early (without
+// the crossings that follow).  Displacements of discrete-interaction points
+// and of the end-of-track deposit are not followed.
 constexpr int ELIST = 48;
 template <class Real>
 struct EList {
     int n;
     int v[ELIST];
-    Real a[ELIST];
+    Real c[ELIST][3];
+    Real k[ELIST];
 };
 template <class Real>
-__device__ inline void elist_close(const Params<Real> &P, EList<Real> &L, Real w_end) {
+__device__ inline void elist_flush(const Params<Real> &P, EList<Real> &L) {
     for (int i = 0; i < L.n; ++i)
-        if (L.a[i] != 0) atomicAdd(P.grad + L.v[i], -(double)(w_end * L.a[i]));
+        if (L.k[i] != 0) atomicAdd(P.grad + L.v[i], (double)(L.k[i] / P.G.rhor[L.v[i]]));
     L.n = 0;
 }
+// a step of displacement d inside voxel ir
 template <class Real>
-__device__ inline void elist_add(const Params<Real> &P, EList<Real> &L, int ir, Real a) {
-    if (L.n > 0 && L.v[L.n - 1] == ir) { L.a[L.n - 1] += a; return; }
-    if (L.n == ELIST) elist_close(P, L, (Real)P.wvox[ir]);
-    L.v[L.n] = ir;
-    L.a[L.n] = a;
-    ++L.n;
+__device__ inline void elist_step(const Params<Real> &P, EList<Real> &L, int ir, Real dx, Real dy, Real dz) {
+    if (L.n == 0 || L.v[L.n - 1] != ir) {
+        if (L.n == ELIST) elist_flush(P, L);
+        L.v[L.n] = ir;
+        L.c[L.n][0] = 0; L.c[L.n][1] = 0; L.c[L.n][2] = 0;
+        L.k[L.n] = 0;
+        ++L.n;
+    }
+    L.c[L.n - 1][0] += dx; L.c[L.n - 1][1] += dy; L.c[L.n - 1][2] += dz;
+}
+// a crossing of a face normal to `axis` with direction component ua
+template <class Real>
+__device__ inline void elist_cross(EList<Real> &L, int axis, Real ua, Real coef) {
+    if (ua == 0) return;
+    const Real f = coef / ua;
+    for (int i = 0; i < L.n; ++i) L.k[i] += f * L.c[i][axis];
 }
 // G_h of the particle's history in an adjoint replay
 template <class Real>
@@ -293,38 +312,44 @@ __device__ inline void push_charged(const Params<Real> &P, const Queue<Real> &qe
 // EGS_XYZGeometry::howfar (egs++/geometry/egs_nd_geometry/egs_nd_geometry.h:963-1104)
 template <class Real>
 __device__ inline int howfar(const Geom<Real> &G, int ireg, Real x, Real y, Real z, Real u, Real v, Real w,
-                             Real &t) {
+                             Real &t, int &axis) {
     const int loc = ireg - G.voff;
-    int iz = loc / G.nxy, ir = loc - iz * G.nxy, iy = ir / G.nx, ix = ir - iy * G.nx;
+    int iz = fdiv(loc, G.mnxy, G.lnxy), ir = loc - iz * G.nxy, iy = fdiv(ir, G.mnx, G.lnx), ix = ir - iy * G.nx;
     int inew = ireg;
     if (u > 0) {
         Real d = (G.xb[ix + 1] - x) / u;
-        if (d <= t) { t = (d <= G.bt) ? G.hbt : d; inew = (ix + 1 < G.nx) ? ireg + 1 : -1; }
+        if (d <= t) { t = (d <= G.bt) ? G.hbt : d; inew = (ix + 1 < G.nx) ? ireg + 1 : -1; axis = 0; }
     } else if (u < 0) {
         Real d = (G.xb[ix] - x) / u;
-        if (d <= t) { t = (d <= G.bt) ? G.hbt : d; inew = (ix - 1 >= 0) ? ireg - 1 : -1; }
+        if (d <= t) { t = (d <= G.bt) ? G.hbt : d; inew = (ix - 1 >= 0) ? ireg - 1 : -1; axis = 0; }
     }
     if (v > 0) {
         Real d = (G.yb[iy + 1] - y) / v;
-        if (d <= t) { t = (d <= G.bt) ? G.hbt : d; inew = (iy + 1 < G.ny) ? ireg + G.nx : -1; }
+        if (d <= t) { t = (d <= G.bt) ? G.hbt : d; inew = (iy + 1 < G.ny) ? ireg + G.nx : -1; axis = 1; }
     } else if (v < 0) {
         Real d = (G.yb[iy] - y) / v;
-        if (d <= t) { t = (d <= G.bt) ? G.hbt : d; inew = (iy - 1 >= 0) ? ireg - G.nx : -1; }
+        if (d <= t) { t = (d <= G.bt) ? G.hbt : d; inew = (iy - 1 >= 0) ? ireg - G.nx : -1; axis = 1; }
     }
     if (w > 0) {
         Real d = (G.zb[iz + 1] - z) / w;
-        if (d <= t) { t = (d <= G.bt) ? G.hbt : d; inew = (iz + 1 < G.nz) ? ireg + G.nxy : -1; }
+        if (d <= t) { t = (d <= G.bt) ? G.hbt : d; inew = (iz + 1 < G.nz) ? ireg + G.nxy : -1; axis = 2; }
     } else if (w < 0) {
         Real d = (G.zb[iz] - z) / w;
-        if (d <= t) { t = (d <= G.bt) ? G.hbt : d; inew = (iz - 1 >= 0) ? ireg - G.nxy : -1; }
+        if (d <= t) { t = (d <= G.bt) ? G.hbt : d; inew = (iz - 1 >= 0) ? ireg - G.nxy : -1; axis = 2; }
     }
     return inew;
+}
+template <class Real>
+__device__ inline int howfar(const Geom<Real> &G, int ireg, Real x, Real y, Real z, Real u, Real v, Real w,
+                             Real &t) {
+    int axis;
+    return howfar(G, ireg, x, y, z, u, v, w, t, axis);
 }
 // EGS_XYZGeometry::hownear (egs_nd_geometry.h:1106-1122)
 template <class Real>
 __device__ inline Real hownear(const Geom<Real> &G, int ireg, Real x, Real y, Real z) {
     const int loc = ireg - G.voff;
-    int iz = loc / G.nxy, ir = loc - iz * G.nxy, iy = ir / G.nx, ix = ir - iy * G.nx;
+    int iz = fdiv(loc, G.mnxy, G.lnxy), ir = loc - iz * G.nxy, iy = fdiv(ir, G.mnx, G.lnx), ix = ir - iy * G.nx;
     Real t = dmin(x - G.xb[ix], G.xb[ix + 1] - x);
     t = dmin(t, dmin(y - G.yb[iy], G.yb[iy + 1] - y));
     t = dmin(t, dmin(z - G.zb[iz], G.zb[iz + 1] - z));
@@ -339,6 +364,145 @@ __device__ inline int plane_where(const Real *b, int n, Real x) {
         if (x < b[mid]) hi = mid; else lo = mid;
     }
     return lo;
+}
+
+
+// ------------------------------------------------ HOWFARLESS geometry ----
+// DOSXYZnrc ihowfarless = 1 in a homogeneous phantom (dosxyznrc.mortran
+// HOWFAR :4177-4200, HOWNEAR :4351-4355): particles see only the phantom's
+// outer faces; voxels matter for scoring alone.
+template <class Real>
+__device__ inline Real hfl_dist_out(const Geom<Real> &G, const Particle<Real> &p) {
+    Real d = (Real)1e20;
+    if (p.u > 0) d = dmin(d, (G.xb[G.nx] - p.x) / p.u); else if (p.u < 0) d = dmin(d, (G.xb[0] - p.x) / p.u);
+    if (p.v > 0) d = dmin(d, (G.yb[G.ny] - p.y) / p.v); else if (p.v < 0) d = dmin(d, (G.yb[0] - p.y) / p.v);
+    if (p.w > 0) d = dmin(d, (G.zb[G.nz] - p.z) / p.w); else if (p.w < 0) d = dmin(d, (G.zb[0] - p.z) / p.w);
+    return d;
+}
+template <class Real>
+__device__ inline Real hfl_hownear(const Geom<Real> &G, const Particle<Real> &p) {
+    Real t = dmin(p.x - G.xb[0], G.xb[G.nx] - p.x);
+    t = dmin(t, dmin(p.y - G.yb[0], G.yb[G.ny] - p.y));
+    return dmin(t, dmin(p.z - G.zb[0], G.zb[G.nz] - p.z));
+}
+template <class Real>
+__device__ inline int hfl_howfar(const Geom<Real> &G, const Particle<Real> &p, Real &t) {
+    Real d = hfl_dist_out(G, p);
+    if (d <= t) { t = (d <= G.bt) ? G.hbt : d; return -1; }
+    return p.ir;
+}
+template <class Real>
+__device__ inline int hfl_index(const Real *b, int n, Real v) {
+    if (v <= b[0]) return 0;
+    if (v >= b[n]) return n - 1;
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (v < b[mid]) hi = mid; else lo = mid;
+    }
+    return lo;
+}
+template <class Real>
+__device__ inline int hfl_locate(const Geom<Real> &G, Real x, Real y, Real z) {
+    return hfl_index(G.xb, G.nx, x) + hfl_index(G.yb, G.ny, y) * G.nx + hfl_index(G.zb, G.nz, z) * G.nxy;
+}
+// HOWFARLESS dose deposition of one charged-particle step
+// (dosxyznrc.mortran:3569-3760): the step from xi0 / ui0 to the particle's
+// end point and direction, of path length tv, becomes two straight segments
+// joined at a hinge placed from the initial or (with equal probability) the
+// final direction -- one straight segment for a step without multiple
+// scattering -- and its energy edep is shared among the voxels the segments
+// cross in proportion to the path length in each.  p.ir holds the start.
+// Returns the voxel at the end of the segments, or -1 when they leave the
+// phantom; `lost` is then the energy past that point, not deposited.
+template <class Real>
+__device__ int hfl_hinge(const Params<Real> &P, Acc<Real> &acc, const Geom<Real> &G, Particle<Real> &p,
+                         const Real xi0[3], const Real ui0[3], Real tv, bool ch_step, Real edep, Real &lost, int &err) {
+    lost = 0;
+    const int loc = p.ir;
+    int iz = fdiv(loc, G.mnxy, G.lnxy), rr = loc - iz * G.nxy, iy = fdiv(rr, G.mnx, G.lnx), ix = rr - iy * G.nx;
+    if (p.x > G.xb[ix] && p.x < G.xb[ix + 1] && p.y > G.yb[iy] && p.y < G.yb[iy + 1] && p.z > G.zb[iz] &&
+        p.z < G.zb[iz + 1]) {
+        deposit(P, acc, loc, p.rng.hist, edep * p.wt);
+        return loc;
+    }
+    const Real d[3] = {p.x - xi0[0], p.y - xi0[1], p.z - xi0[2]};
+    const Real d2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    Real t0 = tv, t1 = 0;
+    Real u0[3] = {ui0[0], ui0[1], ui0[2]}, u1[3] = {0, 0, 0};
+    if (ch_step) {
+        if (urand<Real>(p.rng) < (Real)0.5) {   // hinge from the initial direction
+            Real c = 1 - (d[0] * u0[0] + d[1] * u0[1] + d[2] * u0[2]) / tv;
+            if (c < (Real)1e-3) {
+                t0 = dsqrt(d2);
+                for (int k = 0; k < 3; ++k) u0[k] = d[k] / t0;
+            } else {
+                t0 = (tv * tv - d2) / (2 * tv * c);
+                t1 = tv - t0;
+                for (int k = 0; k < 3; ++k) u1[k] = (d[k] - t0 * u0[k]) / (tv - t0);
+            }
+        } else {                                 // hinge from the final direction
+            u1[0] = p.u; u1[1] = p.v; u1[2] = p.w;
+            Real c = 1 - (d[0] * u1[0] + d[1] * u1[1] + d[2] * u1[2]) / tv;
+            if (c < (Real)1e-3) {
+                t0 = dsqrt(d2);
+                for (int k = 0; k < 3; ++k) u0[k] = d[k] / t0;
+            } else {
+                t1 = (tv * tv - d2) / (2 * tv * c);
+                t0 = tv - t1;
+                for (int k = 0; k < 3; ++k) u0[k] = (d[k] - t1 * u1[k]) / (tv - t1);
+            }
+        }
+    }
+    const Real frac = edep / (t0 + t1);
+    const Real *B[3] = {G.xb, G.yb, G.zb};
+    const int n[3] = {G.nx, G.ny, G.nz}, stride[3] = {1, G.nx, G.nxy};
+    int idx[3] = {ix, iy, iz}, cur = loc;
+    Real pos[3] = {xi0[0], xi0[1], xi0[2]}, done = 0;
+    const int cap = G.nx + G.ny + G.nz + 8;
+#pragma unroll 1
+    for (int s = 0; s < 2; ++s) {
+        const Real ts = s ? t1 : t0;
+        if (!(ts > 0)) continue;
+        const Real *u = s ? u1 : u0;
+        if (s == 1)
+            for (int k = 0; k < 3; ++k) pos[k] += u0[k] * t0;
+        int dir[3];
+        Real dist[3], inv[3];
+        for (int k = 0; k < 3; ++k) {
+            if (u[k] > 0) { inv[k] = 1 / dabs(u[k]); dir[k] = 1; dist[k] = (B[k][idx[k] + 1] - pos[k]) * inv[k]; }
+            else if (u[k] < 0) { inv[k] = 1 / dabs(u[k]); dir[k] = -1; dist[k] = (pos[k] - B[k][idx[k]]) * inv[k]; }
+            else { inv[k] = 0; dir[k] = 0; dist[k] = (Real)1e20; }
+        }
+        Real walked = 0;
+        for (int it = 0;; ++it) {
+            if (it > cap) { err = 1; break; }
+            Real dmax = ts - walked, dl;
+            int a = -1;
+            if (dist[0] < dist[1] && dist[0] < dist[2] && dist[0] < dmax) a = 0;
+            else if (dist[1] < dist[2] && dist[1] < dmax) a = 1;
+            else if (dist[2] < dmax) a = 2;
+            bool out = false;
+            int next = cur;
+            if (a < 0) dl = dmax;
+            else {
+                dl = dist[a];
+                idx[a] += dir[a];
+                if (idx[a] >= 0 && idx[a] < n[a]) {
+                    for (int k = 0; k < 3; ++k) if (k != a) dist[k] -= dl;
+                    next = cur + dir[a] * stride[a];
+                    dist[a] = (B[a][idx[a] + 1] - B[a][idx[a]]) * inv[a];
+                } else out = true;
+            }
+            deposit(P, acc, cur, p.rng.hist, dl * frac * p.wt);
+            done += dl;
+            walked += dl;
+            if (out) { lost = edep - done * frac; return -1; }
+            cur = next;
+            if (walked >= ts) break;
+        }
+    }
+    return cur;
 }
 
 // ------------------------------------------------------------- source ----
@@ -452,7 +616,9 @@ struct PhotonState {
 // v adds G_h / rhor_v: the score of the path's likelihood (all attenuation
 // coefficients scale with rhor, PHOTON's GMFP = GMFPR0 / RHOF), times the
 // history's weighted deposit G_h.
-template <class Real, bool Multi, bool Adj = false>
+// HFL: HOWFARLESS transport (one flight to the interaction or out of the
+// phantom; the voxel is located where the photon interacts).
+template <class Real, bool Multi, bool Adj = false, bool HFL = false>
 __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
     const Tables<Real> &T = P.T;
     const Geom<Real> &G = P.G;
@@ -614,6 +780,15 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
         if (++s.nsteps > STEP_CAP) { err = 1; alive = false; continue; }
         Real gmfp = s.gmfpr0 / s.rhor * s.cohfac;
         Real ustep = gmfp * s.dpmfp;
+        if (HFL) {
+            ++nstep;
+            if (hfl_dist_out(G, p) <= ustep) { esc_tot += (double)(p.E * p.wt); alive = false; continue; }
+            p.x += p.u * ustep; p.y += p.v * ustep; p.z += p.w * ustep;
+            s.dpmfp = 0;
+            p.ir = hfl_locate(G, p.x, p.y, p.z);
+            s.state = 3;
+            continue;
+        }
         int irnew = howfar(geom_of<Real, Multi>(P, p.pb), p.ir, p.x, p.y, p.z, p.u, p.v, p.w, ustep);
         ++nstep;
         if (Adj) gadd(P, ga, p.ir, -Gh * (ustep / gmfp) / s.rhor);
@@ -725,7 +900,8 @@ __device__ inline Real eloss_g(const Tables<Real> &T, const MedScalars<Real> &M,
 // Adj: adjoint replay of the continuous energy loss (see EList); charged
 // secondaries go to the queue (no per-thread stack) so that every lane
 // follows one track at a time.
-template <class Real, bool Multi, bool Adj = false>
+// HFL: HOWFARLESS transport with hinge dose deposition (hfl_hinge).
+template <class Real, bool Multi, bool Adj = false, bool HFL = false>
 __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
     const Tables<Real> &T = P.T;
     const Geom<Real> &G = P.G;
@@ -956,7 +1132,7 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                             rotate(aa, bb, cc, sinthe, costhe, az, g2.u, g2.v, g2.w);
                             q_push(P, P.pout, g1, npush);
                             q_push(P, P.pout, g2, npush);
-                            if (Adj) elist_close(P, el, (Real)0);
+                            if (Adj) elist_flush(P, el);
                             alive = false;
                             continue;
                         }
@@ -1063,6 +1239,10 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
             Real rhof = s.rhor, sig = s.sig0;
             Real tstep;
             const Real *rr = rrow(T, M, s.lelke);
+            // range from the current energy to the lower edge of its bin
+            // ($COMPUTE-DRANGE): serves both tstep and the residual range
+            const Real r0 = drange(T, M, qel, (Real)s.eke, rr[0], s.lelke, (Real)s.elke,
+                                   (s.lelke - (Real)M.eke0) / (Real)M.eke1);
             if (sig <= 0) { tstep = (Real)1e8; s.sig0 = (Real)1e-15; }
             else {
                 if (s.compute_tstep) {
@@ -1074,13 +1254,10 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                         int lelkef = min(max((int)((Real)M.eke1 * elkef + (Real)M.eke0), 1), s.lelke);
                         if (lelkef == s.lelke) tstep = drange(T, M, qel, eke, ekef, s.lelke, elke, elkef);
                         else {
-                            Real ekei = rr[0], elkei = (s.lelke - (Real)M.eke0) / (Real)M.eke1;
-                            Real tuss = drange(T, M, qel, eke, ekei, s.lelke, elke, elkei);
                             const Real *rf = rrow(T, M, lelkef + 1);
-                            ekei = rf[0];
-                            elkei = (lelkef + 1 - (Real)M.eke0) / (Real)M.eke1;
+                            Real ekei = rf[0], elkei = (lelkef + 1 - (Real)M.eke0) / (Real)M.eke1;
                             tstep = drange(T, M, qel, ekei, ekef, lelkef, elkei, elkef);
-                            tstep = tstep + tuss + rr[1 + qel] - rf[1 + qel];
+                            tstep = tstep + r0 + rr[1 + qel] - rf[1 + qel];
                         }
                     }
                     s.total_tstep = tstep;
@@ -1092,16 +1269,11 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
             const Real *row = er.r;
             Real dedx0 = er.dedx(s.elke), dedx = rhof * dedx0;
             Real tmxs = (row[15] * s.elke + row[14]) / rhof;
-            Real range;
-            {
-                Real ekei = rr[0], elkei = (s.lelke - (Real)M.eke0) / (Real)M.eke1;
-                range = drange(T, M, qel, (Real)s.eke, ekei, s.lelke, (Real)s.elke, elkei);
-                range = (range + rr[1 + qel]) / (Real)rhof;
-            }
+            Real range = (r0 + rr[1 + qel]) / (Real)rhof;
             tmxs = dmin(tmxs, T.smaxir);
             Real tustep = (Real)dmin(tstep, dmin((Real)tmxs, range));
             const Geom<Real> &GP = geom_of<Real, Multi>(P, p.pb);
-            Real tperp = hownear(GP, p.ir, p.x, p.y, p.z);
+            Real tperp = HFL ? hfl_hownear(GP, p) : hownear(GP, p.ir, p.x, p.y, p.z);
             Real blccl = rhof * M.blcc;
             Real p2 = s.eke * (s.eke + 2 * rm), beta2 = p2 / (p2 + rm * rm);
             Real ssmfp = beta2 / blccl, skindepth = T.skindepth * ssmfp;
@@ -1133,15 +1305,21 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                 ustep = tustep;
                 callhowfar = !(ustep < tperp);
             }
-            int irold = p.ir, irnew = p.ir;
-            if (callhowfar) irnew = howfar(GP, p.ir, p.x, p.y, p.z, p.u, p.v, p.w, ustep);
+            int irold = p.ir, irnew = p.ir, axis = -1;
+            if (callhowfar) irnew = HFL ? hfl_howfar(GP, p, ustep) : howfar(GP, p.ir, p.x, p.y, p.z, p.u, p.v, p.w, ustep, axis);
+            if (Adj && irnew != irold && axis >= 0) {   // the step ends on a voxel face
+                const Real ua = axis == 0 ? p.u : (axis == 1 ? p.v : p.w);
+                const Real wa = (Real)P.wvox[irold], wb = irnew >= 0 ? (Real)P.wvox[irnew] : (Real)0;
+                elist_step(P, el, irold, p.u * ustep, p.v * ustep, p.w * ustep);
+                elist_cross(el, axis, ua, (wa - wb) * dedx);
+            }
             if (ustep <= 0) ustep = 0;
             if (ustep == 0) {
                 if (irnew != irold) {
                     p.ir = irnew;
                     if (irnew < 0) {
                         esc_tot += (double)((p.iq < 0 ? p.E - rm : p.E + rm) * p.wt);
-                        if (Adj) elist_close(P, el, (Real)0);
+                        if (Adj) elist_flush(P, el);
                         alive = false;
                         continue;
                     }
@@ -1170,12 +1348,23 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                         rotate(p.u, p.v, p.w, sinthe, costhe, az, uf, vf, wf);
                     } else { uf = p.u; vf = p.v; wf = p.w; }
                 }
+                if (HFL) {
+                    const Real xi0[3] = {p.x, p.y, p.z}, ui0[3] = {p.u, p.v, p.w};
+                    p.x = xf; p.y = yf; p.z = zf; p.u = uf; p.v = vf; p.w = wf;
+                    Real lost;
+                    int iend = hfl_hinge(P, acc, GP, p, xi0, ui0, (Real)tvstep, callmsdist, edep, lost, err);
+                    if (iend < 0) {   // the straight segments left the phantom: the particle is gone
+                        Real e = p.E - edep;
+                        edep_part += (edep - lost) * p.wt;
+                        esc_tot += (double)((lost + (p.iq < 0 ? e - rm : e + rm)) * p.wt);
+                        alive = false;
+                        continue;
+                    }
+                    if (irnew >= 0) { p.ir = iend; irold = irnew = iend; }
+                } else
                 deposit(P, acc, p.ir, p.rng.hist, edep * p.wt);   // AUSGAB(0)
-                if (Adj && edep > 0) {
-                    Real a = edep * p.wt / s.rhor;
-                    gadd(P, ga, p.ir, (Real)P.wvox[p.ir] * a);
-                    elist_add(P, el, p.ir, a);
-                }
+                if (Adj && !(irnew != irold && axis >= 0))   // steps inside the voxel (crossings above)
+                    elist_step(P, el, p.ir, xf - p.x, yf - p.y, zf - p.z);
                 edep_part += edep * p.wt;
                 p.x = xf; p.y = yf; p.z = zf; p.u = uf; p.v = vf; p.w = wf;
                 p.E = p.E - edep;
@@ -1189,7 +1378,7 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                         p.ir = irnew;
                         if (irnew < 0) {
                             esc_tot += (double)((p.iq < 0 ? p.E - rm : p.E + rm) * p.wt);
-                            if (Adj) elist_close(P, el, (Real)0);
+                            if (Adj) elist_flush(P, el);
                             alive = false;
                             continue;
                         }
@@ -1222,7 +1411,7 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
             Real edep = p.E - rm;
             deposit(P, acc, p.ir, p.rng.hist, edep * p.wt);
             edep_tot += (double)(edep * p.wt);
-            if (Adj) elist_close(P, el, (Real)P.wvox[p.ir]);
+            if (Adj) elist_flush(P, el);
             if (p.iq > 0) annih_at_rest(P, P.pout, p, npush, err);
             alive = false;
         }
@@ -1278,6 +1467,20 @@ namespace {
             return EGSGPU_ERR_CUDA;                                                           \
         }                                                                                     \
     } while (0)
+
+// Multiplier and shift for dividing by d with a multiply-high, an add and a
+// shift: l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1; then
+// n / d = (umulhi(n, m) + n) >> l for 0 <= n < 2^31 (the sum cannot overflow).
+static void fast_divisor(uint32_t d, uint32_t &m, int &l) {
+    l = 0;
+    while ((1ull << l) < d) ++l;
+    m = (uint32_t)((((1ull << 32) * ((1ull << l) - d)) / d) + 1);
+}
+template <class Real>
+static void set_divisors(Geom<Real> &g) {
+    fast_divisor((uint32_t)g.nx, g.mnx, g.lnx);
+    fast_divisor((uint32_t)g.nxy, g.mnxy, g.lnxy);
+}
 
 struct DevMem {
     void *p = nullptr;
@@ -1447,6 +1650,8 @@ struct Engine : EngineBase {
             return cudaMemcpy(d.p, src, bytes, cudaMemcpyHostToDevice);
         };
         CK(up(d_etab, etab.data(), etab.size() * sizeof(Real)));
+        h_etab = etab;
+        hatch_ = &H;
         CK(up(d_erange, erange.data(), erange.size() * sizeof(Real)));
         CK(up(d_gtab, gtab.data(), gtab.size() * sizeof(Real)));
         CK(up(d_pmax, pmax.data(), pmax.size() * sizeof(Real)));
@@ -1476,10 +1681,41 @@ struct Engine : EngineBase {
         return 0;
     }
 
+    // HOWFARLESS: the phantom must be one medium at one density; the step
+    // limits use the smallest voxel dimension (egs_hatch.cpp howfarless_tmxs)
+    bool homogeneous = false;
+    double mindel = 0, hfl_mindel = -1;
+    const egs::Hatch *hatch_ = nullptr;
+    std::vector<Real> h_etab;
+    DevMem d_etab_hfl;
+
+    int hfl_tables(std::string &err) {
+        if (hfl_mindel == mindel && d_etab_hfl.p) return 0;
+        std::vector<Real> e = h_etab;
+        for (int im = 0; im < nmed; ++im) {
+            std::vector<double> t0, t1;
+            egs::howfarless_tmxs(hatch_->media[im], hatch_->params, mindel, t0, t1);
+            for (int i = 0; i < hatch_->media[im].meke; ++i) {
+                e[((size_t)meds[im].etab_off + i) * 16 + 14] = (Real)t0[i];
+                e[((size_t)meds[im].etab_off + i) * 16 + 15] = (Real)t1[i];
+            }
+        }
+        CK(d_etab_hfl.alloc(e.size() * sizeof(Real)));
+        CK(cudaMemcpy(d_etab_hfl.p, e.data(), e.size() * sizeof(Real), cudaMemcpyHostToDevice));
+        hfl_mindel = mindel;
+        return 0;
+    }
+
     int geometry(int nx, int ny, int nz, const double *xb, const double *yb, const double *zb, const int32_t *med,
                  const double *rhor, std::string &err) override {
         nprob = 0;
         nvox = (long long)nx * ny * nz;
+        homogeneous = true;
+        for (long long i = 1; i < nvox && homogeneous; ++i) homogeneous = med[i] == med[0] && rhor[i] == rhor[0];
+        mindel = 1e30;
+        for (int i = 0; i < nx; ++i) mindel = std::min(mindel, xb[i + 1] - xb[i]);
+        for (int i = 0; i < ny; ++i) mindel = std::min(mindel, yb[i + 1] - yb[i]);
+        for (int i = 0; i < nz; ++i) mindel = std::min(mindel, zb[i + 1] - zb[i]);
         std::vector<Real> x(xb, xb + nx + 1), y(yb, yb + ny + 1), z(zb, zb + nz + 1), r(nvox);
         std::vector<uint8_t> m(nvox);
         for (long long i = 0; i < nvox; ++i) { m[i] = (uint8_t)med[i]; r[i] = (Real)rhor[i]; }
@@ -1500,6 +1736,7 @@ struct Engine : EngineBase {
         G.bt = sizeof(Real) == 8 ? (Real)(1.0 / 4294967296.0) : (Real)(1.0 / 2097152.0);
         G.hbt = G.bt / 2;
         G.voff = 0;
+        set_divisors(G);
         CK(d_dose.alloc(nvox * sizeof(double)));
         CK(d_sum.alloc(nvox * sizeof(double)));
         CK(d_sum2.alloc(nvox * sizeof(double)));
@@ -1552,7 +1789,8 @@ struct Engine : EngineBase {
     cudaEvent_t ev_in = nullptr;
     bool graph_ok = true;
 
-    cudaError_t enqueue_rounds(const Params<Real> &P0, int grid, int bs, bool events, bool multi, bool adj = false) {
+    cudaError_t enqueue_rounds(const Params<Real> &P0, int grid, int bs, bool events, bool multi, bool adj = false,
+                               bool hfl = false) {
         unsigned *counts = (unsigned *)d_counts.p;
         cudaError_t e = cudaSuccess;
         for (int r = 0; r < ROUNDS && e == cudaSuccess; ++r) {
@@ -1562,13 +1800,15 @@ struct Engine : EngineBase {
             if ((e = cudaMemsetAsync(counts + 2 * nxt, 0, 2 * sizeof(unsigned), ws))) break;
             if ((e = cudaMemsetAsync(counts + 4 + 2 * nxt, 0, 2 * sizeof(unsigned), ws))) break;
             if (events && (e = cudaEventRecord(gev[4 * r], ws))) break;
-            if (adj) k_photon<Real, false, true><<<grid, bs, 0, ws>>>(P);
+            if (hfl) k_photon<Real, false, false, true><<<grid, bs, 0, ws>>>(P);
+            else if (adj) k_photon<Real, false, true><<<grid, bs, 0, ws>>>(P);
             else if (multi) k_photon<Real, true><<<grid, bs, 0, ws>>>(P);
             else k_photon<Real, false><<<grid, bs, 0, ws>>>(P);
             if ((e = cudaGetLastError())) break;
             if (events && (e = cudaEventRecord(gev[4 * r + 1], ws))) break;
             if (events && (e = cudaEventRecord(gev[4 * r + 2], ws))) break;
-            if (adj) k_electron<Real, false, true><<<grid, bs, 0, ws>>>(P);
+            if (hfl) k_electron<Real, false, false, true><<<grid, bs, 0, ws>>>(P);
+            else if (adj) k_electron<Real, false, true><<<grid, bs, 0, ws>>>(P);
             else if (multi) k_electron<Real, true><<<grid, bs, 0, ws>>>(P);
             else k_electron<Real, false><<<grid, bs, 0, ws>>>(P);
             if ((e = cudaGetLastError())) break;
@@ -1579,14 +1819,14 @@ struct Engine : EngineBase {
 
     // Captures the rounds (without events) into a graph; on any failure the
     // engine keeps launching directly.
-    void build_graph(const Params<Real> &P0, int grid, int bs, bool multi) {
+    void build_graph(const Params<Real> &P0, int grid, int bs, bool multi, bool hfl) {
         if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
         if (cudaStreamBeginCapture(ws, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
             cudaGetLastError();
             graph_ok = false;
             return;
         }
-        cudaError_t e = enqueue_rounds(P0, grid, bs, false, multi);
+        cudaError_t e = enqueue_rounds(P0, grid, bs, false, multi, false, hfl);
         cudaGraph_t g = nullptr;
         cudaError_t e2 = cudaStreamEndCapture(ws, &g);
         if (e == cudaSuccess && e2 == cudaSuccess && g) e = cudaGraphInstantiate(&gexec, g, 0);
@@ -1650,7 +1890,14 @@ struct Engine : EngineBase {
         // persistent grids: never more CTAs than can be resident at once
         int occ_p = 1, occ_e = 1;
         const bool adj = mode && mode->adj;
-        if (adj) {
+        const bool hfl = cfg.howfarless > 0;
+        if (hfl && (Multi || mode)) { err = "HOWFARLESS transport is for one homogeneous phantom (no adjoint)"; return EGSGPU_ERR_ARG; }
+        if (hfl && !homogeneous) { err = "HOWFARLESS transport needs a homogeneous phantom"; return EGSGPU_ERR_ARG; }
+        if (hfl) {
+            if (int rc = hfl_tables(err)) return rc;
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, false, false, true>, bs, 0));
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, false, false, true>, bs, 0));
+        } else if (adj) {
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, false, true>, bs, 0));
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, false, true>, bs, 0));
         } else {
@@ -1662,6 +1909,7 @@ struct Engine : EngineBase {
         Params<Real> P;
         std::memset(&P, 0, sizeof(P));
         P.T = T; P.G = G;
+        if (hfl) P.T.etab = (const Real *)d_etab_hfl.p;
         P.dose = (double *)d_dose.p;
         P.hist_tally = (!Multi && hist_n > 0) ? (double *)d_hist.p : nullptr;
         P.hist_first = hist_first; P.hist_n = hist_n;
@@ -1686,7 +1934,7 @@ struct Engine : EngineBase {
         }
         P.pin = q[0]; P.ein = q[2]; P.pout = q[0]; P.eout = q[2];
         const bool use_graph = cfg.use_graph > 0 && graph_ok && !mode;
-        if (use_graph) build_graph(P, grid, bs, Multi);
+        if (use_graph) build_graph(P, grid, bs, Multi, hfl);
         const bool graph = use_graph && gexec;
         unsigned *counts = (unsigned *)d_counts.p;
         CK(cudaEventRecord(ev_in, st));
@@ -1723,7 +1971,7 @@ struct Engine : EngineBase {
                 bool done = false;
                 for (int rep = 0; rep < 100000 / ROUNDS && !done; ++rep) {
                     if (graph) CK(cudaGraphLaunch(gexec, ws));
-                    else CK(enqueue_rounds(P, grid, bs, true, Multi, adj));
+                    else CK(enqueue_rounds(P, grid, bs, true, Multi, adj, hfl));
                     CK(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, ws));
                     CK(cudaStreamSynchronize(ws));
                     if (rep == 0) { prof_ms[0] += elapsed(ev[0], ev[1]); ++prof_n[0]; }
@@ -1879,6 +2127,7 @@ struct Engine : EngineBase {
             g.med = (const uint8_t *)d_med.p; g.rhor = (const Real *)d_rhor.p;
             g.bt = bt; g.hbt = bt / 2;
             g.voff = voff[k];
+            set_divisors(g);
             seeds[k] = pd[k].seed;
             phist[k] = pd[k].histories;
         }
@@ -1891,6 +2140,7 @@ struct Engine : EngineBase {
         G = gs[0];
         nvox = tot;
         nprob = n;
+        homogeneous = false;
         pdone.assign(n, 0);
         CK(d_dose.alloc(nvox * sizeof(double)));
         CK(d_sum.alloc(nvox * sizeof(double)));

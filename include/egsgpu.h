@@ -54,6 +54,13 @@ typedef struct {
     int inter_batch;      /* lanes of a warp due to interact before their interactions
                              are sampled together; 0 = default (12), -1 = immediately
                              (results are identical either way) */
+    int howfarless;       /* 1: DOSXYZnrc HOWFARLESS transport (ihowfarless,
+                             user_codes/dosxyznrc/dosxyznrc.mortran:425-455) for a
+                             homogeneous phantom: particles see only its outer
+                             faces, charged-particle steps deposit along a two-segment
+                             hinge path, step limits floored at half the smallest
+                             voxel size.  Refused for inhomogeneous phantoms, several
+                             phantoms and the adjoint. */
 } egsgpu_config;
 
 /* Source: egs++ EGS_ParallelBeam (sources/egs_parallel_beam) with a point

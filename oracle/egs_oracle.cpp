@@ -173,6 +173,10 @@ struct Oracle {
     Source S;
     double ecut = 0.521, pcut = 0.01;
     std::string err;
+    // HOWFARLESS (DOSXYZnrc ihowfarless = 1): transport against the outer
+    // boundary only, with the floored step limits of modify_tmxs per medium
+    bool hfl = false;
+    std::vector<std::vector<double>> hfl_t0, hfl_t1;
 };
 
 // --------------------------------------------------------- RNG access ----
@@ -268,6 +272,137 @@ int is_where(const Geometry &G, double x, double y, double z) {
     int iy = plane_where(G.yb, y); if (iy < 0) return -1;
     int iz = plane_where(G.zb, z); if (iz < 0) return -1;
     return ix + iy * G.nx + iz * G.nxy;
+}
+
+// ------------------------------------------------- HOWFARLESS geometry ----
+// DOSXYZnrc HOWFAR / HOWNEAR with howfarless (dosxyznrc.mortran:4177-4200,
+// :4351-4355): distances to the phantom's outer faces only.
+double hfl_dist_out(const Geometry &G, const Particle &p) {
+    double d = 1e20;
+    if (p.u > 0) d = std::min(d, (G.xb[G.nx] - p.x) / p.u); else if (p.u < 0) d = std::min(d, (G.xb[0] - p.x) / p.u);
+    if (p.v > 0) d = std::min(d, (G.yb[G.ny] - p.y) / p.v); else if (p.v < 0) d = std::min(d, (G.yb[0] - p.y) / p.v);
+    if (p.w > 0) d = std::min(d, (G.zb[G.nz] - p.z) / p.w); else if (p.w < 0) d = std::min(d, (G.zb[0] - p.z) / p.w);
+    return d;
+}
+double hfl_hownear(const Geometry &G, const Particle &p) {
+    double t = std::min(p.x - G.xb[0], G.xb[G.nx] - p.x);
+    t = std::min(t, std::min(p.y - G.yb[0], G.yb[G.ny] - p.y));
+    return std::min(t, std::min(p.z - G.zb[0], G.zb[G.nz] - p.z));
+}
+int hfl_howfar(const Geometry &G, const Particle &p, double &t) {
+    double d = hfl_dist_out(G, p);
+    if (d <= t) { t = (d <= G.bt) ? G.hbt : d; return -1; }
+    return p.ir;
+}
+// voxel holding a point, indices clamped into the phantom
+int hfl_locate(const Geometry &G, double x, double y, double z) {
+    auto idx = [](const std::vector<double> &b, double v) {
+        int n = (int)b.size() - 1;
+        if (v <= b[0]) return 0;
+        if (v >= b[n]) return n - 1;
+        int lo = 0, hi = n;
+        while (hi - lo > 1) { int mid = (lo + hi) / 2; if (v < b[mid]) hi = mid; else lo = mid; }
+        return lo;
+    };
+    return idx(G.xb, x) + idx(G.yb, y) * G.nx + idx(G.zb, z) * G.nxy;
+}
+
+// HOWFARLESS dose deposition of one charged-particle step
+// (dosxyznrc.mortran:3569-3760).  The step from (xi, ui) to the particle's
+// end point (p.x, ...) with end direction (p.u, ...) and path length tv is
+// replaced by two straight segments joined at a hinge -- placed, with equal
+// probability, from the initial or from the final direction; a step without
+// multiple scattering is one straight segment -- and the step's energy edep
+// is shared among the voxels the segments cross in proportion to the path
+// length in each.  p.ir is the voxel holding the start.  Returns the voxel
+// where the segments end, or -1 when they leave the phantom; `lost` receives
+// the energy beyond that point, which is not deposited.
+int hfl_hinge(Run &R, Particle &p, const Geometry &G, const double xi0[3], const double ui0[3], double tv,
+              bool ch_step, double edep, double &lost) {
+    lost = 0;
+    int loc = p.ir, iz = loc / G.nxy, rr = loc - iz * G.nxy, iy = rr / G.nx, ix = rr - iy * G.nx;
+    const double pe[3] = {p.x, p.y, p.z}, ue[3] = {p.u, p.v, p.w};
+    if (pe[0] > G.xb[ix] && pe[0] < G.xb[ix + 1] && pe[1] > G.yb[iy] && pe[1] < G.yb[iy + 1] &&
+        pe[2] > G.zb[iz] && pe[2] < G.zb[iz + 1]) {   // the whole step stays in the voxel
+        score(R, p.ir, edep, p.wt);
+        score_hist(R, p, edep * p.wt);
+        return p.ir;
+    }
+    double d[3] = {pe[0] - xi0[0], pe[1] - xi0[1], pe[2] - xi0[2]};
+    double d2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    double t[2] = {tv, 0}, u[2][3] = {{ui0[0], ui0[1], ui0[2]}, {0, 0, 0}};
+    if (ch_step) {
+        if (rnd(R, p) < 0.5) {   // hinge from the initial direction
+            double c = 1 - (d[0] * u[0][0] + d[1] * u[0][1] + d[2] * u[0][2]) / tv;
+            if (c < 1e-3) {
+                t[0] = std::sqrt(d2);
+                for (int k = 0; k < 3; ++k) u[0][k] = d[k] / t[0];
+                t[1] = 0;
+            } else {
+                t[0] = (tv * tv - d2) / (2 * tv * c);
+                t[1] = tv - t[0];
+                for (int k = 0; k < 3; ++k) u[1][k] = (d[k] - t[0] * u[0][k]) / (tv - t[0]);
+            }
+        } else {                 // hinge from the final direction
+            for (int k = 0; k < 3; ++k) u[1][k] = ue[k];
+            double c = 1 - (d[0] * u[1][0] + d[1] * u[1][1] + d[2] * u[1][2]) / tv;
+            if (c < 1e-3) {
+                t[0] = std::sqrt(d2);
+                for (int k = 0; k < 3; ++k) u[0][k] = d[k] / t[0];
+                t[1] = 0;
+            } else {
+                t[1] = (tv * tv - d2) / (2 * tv * c);
+                t[0] = tv - t[1];
+                for (int k = 0; k < 3; ++k) u[0][k] = (d[k] - t[1] * u[1][k]) / (tv - t[1]);
+            }
+        }
+    }
+    const double ttot = t[0] + t[1], frac = edep / ttot;
+    const std::vector<double> *B[3] = {&G.xb, &G.yb, &G.zb};
+    const int n[3] = {G.nx, G.ny, G.nz}, stride[3] = {1, G.nx, G.nxy};
+    int idx[3] = {ix, iy, iz}, cur = loc;
+    double pos[3] = {xi0[0], xi0[1], xi0[2]}, done = 0;
+    for (int s = 0; s < 2; ++s) {
+        if (!(t[s] > 0)) continue;
+        if (s == 1)
+            for (int k = 0; k < 3; ++k) pos[k] += u[0][k] * t[0];
+        int dir[3];
+        double dist[3], inv[3];
+        for (int k = 0; k < 3; ++k) {
+            const std::vector<double> &b = *B[k];
+            if (u[s][k] > 0) { inv[k] = 1 / std::fabs(u[s][k]); dir[k] = 1; dist[k] = (b[idx[k] + 1] - pos[k]) * inv[k]; }
+            else if (u[s][k] < 0) { inv[k] = 1 / std::fabs(u[s][k]); dir[k] = -1; dist[k] = (pos[k] - b[idx[k]]) * inv[k]; }
+            else { inv[k] = 0; dir[k] = 0; dist[k] = 1e20; }
+        }
+        double walked = 0;
+        while (true) {
+            double dmax = t[s] - walked, dl;
+            int a = -1;
+            if (dist[0] < dist[1] && dist[0] < dist[2] && dist[0] < dmax) a = 0;
+            else if (dist[1] < dist[2] && dist[1] < dmax) a = 1;
+            else if (dist[2] < dmax) a = 2;
+            bool out = false;
+            int next = cur;
+            if (a < 0) dl = dmax;
+            else {
+                dl = dist[a];
+                idx[a] += dir[a];
+                if (idx[a] >= 0 && idx[a] < n[a]) {
+                    for (int k = 0; k < 3; ++k) if (k != a) dist[k] -= dl;
+                    next = cur + dir[a] * stride[a];
+                    dist[a] = ((*B[a])[idx[a] + 1] - (*B[a])[idx[a]]) * inv[a];
+                } else out = true;
+            }
+            score(R, cur, dl * frac, p.wt);
+            score_hist(R, p, dl * frac * p.wt);
+            done += dl;
+            walked += dl;
+            if (out) { lost = edep - done * frac; return -1; }
+            cur = next;
+            if (walked >= t[s]) break;
+        }
+    }
+    return cur;
 }
 
 // egs_nd_geometry.h:1281-1379: entry from outside; returns region, t updated.
@@ -874,6 +1009,14 @@ void photon(Run &R) {
                 pc.cohfac = m.cohe1[l] * pc.gle + m.cohe0[l];
                 gmfp *= pc.cohfac;
                 double tstep = gmfp * dpmfp, ustep = tstep;
+                if (O.hfl) {   // one flight to the interaction or out of the phantom
+                    R.T->steps += 1; R.T->psteps += 1;
+                    if (hfl_dist_out(G, p) <= ustep) { escape(R, p, p.E); return; }
+                    p.x += p.u * ustep; p.y += p.v * ustep; p.z += p.w * ustep;
+                    p.ir = hfl_locate(G, p.x, p.y, p.z);   // the voxel that scores the interaction
+                    interact = true;
+                    break;
+                }
                 int irnew = howfar(G, p.ir, p, ustep);
                 R.T->steps += 1; R.T->psteps += 1;
                 p.x += p.u * ustep; p.y += p.v * ustep; p.z += p.w * ustep;
@@ -999,7 +1142,8 @@ newelectron:
                 tstep = total_tstep / rhof;
             }
             double dedx0 = em.dedx(elke, lelke - 1), dedx = rhof * dedx0;
-            double tmxs = (m.tmxs1[lelke - 1] * elke + m.tmxs0[lelke - 1]) / rhof;
+            double tmxs = O.hfl ? (O.hfl_t1[medium][lelke - 1] * elke + O.hfl_t0[medium][lelke - 1]) / rhof
+                                : (m.tmxs1[lelke - 1] * elke + m.tmxs0[lelke - 1]) / rhof;
             {
                 double ekei = m.E_array[lelke - 1], elkei = (lelke - m.eke0) / m.eke1;
                 range = drange(em, eke, ekei, lelke, elke, elkei);
@@ -1007,7 +1151,7 @@ newelectron:
             }
             tmxs = std::min(tmxs, P.smaxir);
             double tustep = std::min(tstep, std::min(tmxs, range));
-            double tperp = hownear(G, p.ir, p);
+            double tperp = O.hfl ? hfl_hownear(G, p) : hownear(G, p.ir, p);
             double blccl = rhof * m.blcc;
             double p2 = eke * (eke + RMT2), beta2 = p2 / (p2 + RMSQ);
             double ssmfp = beta2 / blccl, skindepth = P.skindepth_for_bca * ssmfp;
@@ -1038,7 +1182,7 @@ newelectron:
                 callhowfar = !(ustep < tperp);
             }
             int irold = p.ir, irnew = p.ir;
-            if (callhowfar) irnew = howfar(G, p.ir, p, ustep);
+            if (callhowfar) irnew = O.hfl ? hfl_howfar(G, p, ustep) : howfar(G, p.ir, p, ustep);
             if (ustep <= 0) ustep = 0;
             if (ustep == 0) {
                 if (irnew != irold) {
@@ -1082,8 +1226,21 @@ newelectron:
                     rotate(p.u, p.v, p.w, sinthe, costhe, az, uf, vf, wf);
                 } else { uf = p.u; vf = p.v; wf = p.w; }
             }
-            deposit(R, p, edep);   // AUSGAB(0) in the region before transport
-            p.x = xf; p.y = yf; p.z = zf; p.u = uf; p.v = vf; p.w = wf;
+            if (O.hfl) {
+                const double xi0[3] = {p.x, p.y, p.z}, ui0[3] = {p.u, p.v, p.w};
+                p.x = xf; p.y = yf; p.z = zf; p.u = uf; p.v = vf; p.w = wf;
+                double lost;
+                int iend = hfl_hinge(R, p, G, xi0, ui0, tvstep, callmsdist, edep, lost);
+                if (iend < 0) {   // the straight segments left the phantom: the particle is gone
+                    double e = peie - edep;
+                    escape(R, p, lost + ((lelec < 0) ? e - RM : e + RM));
+                    return;
+                }
+                if (irnew >= 0) { p.ir = iend; irold = irnew = iend; }
+            } else {
+                deposit(R, p, edep);   // AUSGAB(0) in the region before transport
+                p.x = xf; p.y = yf; p.z = zf; p.u = uf; p.v = vf; p.w = wf;
+            }
             peie = peie - edep;
             eie = peie;
             p.E = peie;
@@ -1451,6 +1608,27 @@ int oracle_set_geometry(oracle_handle *h, int nx, int ny, int nz, const double *
     for (size_t i = 0; i < nv; ++i)
         if (G.med[i] < 0 || G.med[i] >= (int)h->O.H.media.size()) return 1;
     h->T.batch.assign(nv, 0); h->T.sum.assign(nv, 0); h->T.sum2.assign(nv, 0);
+    return 0;
+}
+
+// HOWFARLESS transport (on != 0) in the current, homogeneous phantom: call
+// after oracle_set_geometry.
+int oracle_set_howfarless(oracle_handle *h, int on) {
+    Oracle &O = h->O;
+    O.hfl = on != 0;
+    O.hfl_t0.clear();
+    O.hfl_t1.clear();
+    if (!O.hfl) return 0;
+    double mindel = 1e30;
+    for (int i = 0; i < O.G.nx; ++i) mindel = std::min(mindel, O.G.xb[i + 1] - O.G.xb[i]);
+    for (int i = 0; i < O.G.ny; ++i) mindel = std::min(mindel, O.G.yb[i + 1] - O.G.yb[i]);
+    for (int i = 0; i < O.G.nz; ++i) mindel = std::min(mindel, O.G.zb[i + 1] - O.G.zb[i]);
+    for (const Medium &m : O.H.media) {
+        std::vector<double> t0, t1;
+        howfarless_tmxs(m, O.H.params, mindel, t0, t1);
+        O.hfl_t0.push_back(t0);
+        O.hfl_t1.push_back(t1);
+    }
     return 0;
 }
 

@@ -28,6 +28,7 @@ def lib():
         L.oracle_destroy.argtypes = [vp]
         L.oracle_set_geometry.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp, dp, dp, C.POINTER(C.c_int32), dp]
         L.oracle_set_source.argtypes = [vp, C.c_void_p]
+        L.oracle_set_howfarless.argtypes = [vp, C.c_int]
         L.oracle_run.argtypes = [vp, i64, i64, C.c_int, C.c_uint32, C.c_int, C.c_int]
         L.oracle_set_history_tally.argtypes = [vp, i64, i64]
         L.oracle_get_history_tally.argtypes = [vp, dp]
@@ -65,6 +66,10 @@ class Oracle:
                                         g.med.ctypes.data_as(C.POINTER(C.c_int32)), _dp(g.rhor))
         if rc:
             raise RuntimeError("oracle: bad geometry")
+
+    def set_howfarless(self, on=True):
+        """DOSXYZnrc HOWFARLESS transport in the current (homogeneous) phantom."""
+        assert self.L.oracle_set_howfarless(self.h, int(bool(on))) == 0
 
     def set_source(self, src):
         self.src = src

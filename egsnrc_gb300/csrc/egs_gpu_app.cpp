@@ -57,6 +57,42 @@ static bool planes(const Item *g, const char *p, const char *s, std::vector<doub
     return false;
 }
 
+// BEAMnrc phase-space file (egs++/sources/egs_phsp_source/egs_phsp_source.cpp:
+// header :64-130, records :360-423): "MODE0"/"MODE2", counts, energies, then
+// LATCH (bit 30 e-, bit 29 e+), E (total for charged, < 0 for a new history),
+// X, Y, U, V, WT (< 0 when W < 0) [, ZLAST].  Fills 7 floats per particle:
+// charge, kinetic energy, x, y, u, v, weight.
+static bool read_egsphsp(const std::string &path, std::vector<float> &out, double &incident, std::string &err) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) { err = "cannot open phase-space file " + path; return false; }
+    char mode[5];
+    f.read(mode, 5);
+    int rec = std::string(mode, 5) == "MODE0" ? 28 : (std::string(mode, 5) == "MODE2" ? 32 : 0);
+    if (!rec) { err = path + ": not an egsphsp file"; return false; }
+    int32_t n = 0, nphot = 0;
+    float ekmax = 0, ekmin = 0, ninc = 0;
+    f.read((char *)&n, 4); f.read((char *)&nphot, 4);
+    f.read((char *)&ekmax, 4); f.read((char *)&ekmin, 4); f.read((char *)&ninc, 4);
+    incident = ninc;
+    f.seekg(rec, std::ios::beg);
+    out.resize((size_t)n * 7);
+    std::vector<char> buf(rec);
+    for (int32_t i = 0; i < n; ++i) {
+        if (!f.read(buf.data(), rec)) { err = path + ": truncated"; return false; }
+        uint32_t latch;
+        float v[6];
+        std::memcpy(&latch, buf.data(), 4);
+        std::memcpy(v, buf.data() + 4, 24);
+        float q = (latch & (1u << 30)) ? -1.0f : ((latch & (1u << 29)) ? 1.0f : 0.0f);
+        double e = std::fabs(v[0]);
+        float *o = &out[(size_t)i * 7];
+        o[0] = q;
+        o[1] = (float)(q != 0 ? e - 0.5109989461 : e);
+        o[2] = v[1]; o[3] = v[2]; o[4] = v[3]; o[5] = v[4]; o[6] = v[5];
+    }
+    return true;
+}
+
 static const char *MEDCH = "123456789ABCDEFGHIJKLMNOPQRSTUVWXYZabcdefghijklmnopqrstuvwxyz";
 
 static bool read_egsphant(const std::string &path, Phantom &P, std::string &err) {
@@ -221,9 +257,56 @@ int main(int argc, char **argv) {
     for (auto *b : sd->blocks("source"))
         if (egsin::norm(b->get("name")) == egsin::norm(sname)) s = b;
     if (!s) return fail("simulation source '" + sname + "' not defined");
-    if (egsin::norm(s->get("library")) != "egs_parallel_beam") return fail("only egs_parallel_beam sources are supported");
     egsgpu_source src;
     std::memset(&src, 0, sizeof(src));
+    // EGS_TransformedSource (egs++/sources/egs_transformed_source) with a
+    // translation: the inner source's particles are shifted
+    double shift[3] = {0, 0, 0};
+    if (egsin::norm(s->get("library")) == "egs_transformed_source") {
+        const Item *t = s->block("transformation");
+        if (t) {
+            if (t->has("rotation") || t->has("rotation vector")) return fail("rotated sources are not supported");
+            auto v = Item::numbers(t->get("translation", "0 0 0"));
+            for (int k = 0; k < 3 && k < (int)v.size(); ++k) shift[k] = v[k];
+        }
+        std::string inner = s->get("source name");
+        const Item *in = nullptr;
+        for (auto *b : sd->blocks("source"))
+            if (egsin::norm(b->get("name")) == egsin::norm(inner)) in = b;
+        if (!in) return fail("source '" + inner + "' not defined");
+        s = in;
+    }
+    std::vector<float> phsp;
+    std::string lib = egsin::norm(s->get("library"));
+    if (lib == "egs_phsp_source") {
+        // EGS_PhspSource (egs_phsp_source.cpp:196-280): particle type, cutout
+        // and recycling; rejected particles keep their place with weight 0
+        double incident = 0;
+        std::string perr;
+        if (!read_egsphsp(s->get("phase space file"), phsp, incident, perr)) return fail(perr);
+        std::string pt = egsin::norm(s->get("particle type", "all"));
+        int want = pt == "photons" ? 0 : pt == "electrons" ? -1 : pt == "positrons" ? 1 : pt == "charged" ? 2 : 3;
+        if (want == 3 && pt != "all") return fail("unknown particle type '" + pt + "'");
+        auto cut = Item::numbers(s->get("cutout", ""));
+        int rp = (int)s->num("recycle photons", 0), re = (int)s->num("recycle electrons", 0);
+        if (rp != re) return fail("different recycle numbers for photons and electrons are not supported");
+        for (size_t i = 0; i < phsp.size(); i += 7) {
+            float q = phsp[i];
+            bool keep = want == 3 || (want == 2 ? q != 0 : q == (float)want);
+            if (cut.size() == 4 && (phsp[i + 2] < cut[0] || phsp[i + 2] > cut[1] || phsp[i + 3] < cut[2] ||
+                                    phsp[i + 3] > cut[3]))
+                keep = false;
+            if (!keep) phsp[i + 6] = phsp[i + 6] < 0 ? -0.0f : 0.0f;
+        }
+        src.shape = 2;
+        src.nphsp = (long long)(phsp.size() / 7);
+        src.phsp = phsp.data();
+        src.recycle = rp;
+        for (int k = 0; k < 3; ++k) src.pos[k] = shift[k];
+        src.dir[2] = 1;
+        std::printf("phase space: %lld particles, %.0f incident histories\n", src.nphsp, incident);
+    } else if (lib != "egs_parallel_beam") return fail("only egs_parallel_beam and egs_phsp_source sources are supported");
+    if (lib == "egs_parallel_beam") {
     src.charge = (int)s->num("charge", 0);
     auto dir = Item::numbers(s->get("direction", "0 0 1"));
     for (int k = 0; k < 3; ++k) src.dir[k] = k < (int)dir.size() ? dir[k] : 0;
@@ -265,6 +348,9 @@ int main(int argc, char **argv) {
         src.edges = edges.data();
         src.weights = weights.data();
     } else return fail("spectrum type '" + sp->get("type") + "' is not supported");
+    for (int k = 0; k < 3; ++k) src.pos[k] += shift[k];
+    src.xmin += shift[0]; src.xmax += shift[0]; src.ymin += shift[1]; src.ymax += shift[1];
+    }
     if ((st = egsgpu_set_source(h, &src))) return fail(egsgpu_last_error(h));
 
     uint32_t seed = 1;

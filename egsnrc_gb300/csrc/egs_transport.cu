@@ -897,9 +897,7 @@ __device__ inline Real eloss_g(const Tables<Real> &T, const MedScalars<Real> &M,
     return de + eke - eketmp;
 }
 
-// Adj: adjoint replay of the continuous energy loss (see EList); charged
-// secondaries go to the queue (no per-thread stack) so that every lane
-// follows one track at a time.
+// Adj: adjoint replay of the continuous energy loss (see EList).
 // HFL: HOWFARLESS transport with hinge dose deposition (hfl_hinge).
 template <class Real, bool Multi, bool Adj = false, bool HFL = false>
 __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
@@ -921,6 +919,10 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
     AccG<Real> ga{-1, (Real)0};
     EList<Real> el;
     el.n = 0;
+    // adjoint: the voxel-visit lists of suspended particles; a secondary
+    // starts from a copy of its parent's list (chords to its creation point,
+    // coefficients zero), so that its crossings also see the parent's path
+    EList<Real> elstack[Adj ? LSTACK : 1];
     bool alive = false, exhausted = false;
     unsigned long long nstep = 0, npush = 0, ninter = 0, lanes = 0, iters = 0;
     int inter_wait = 0;   // warp-uniform iterations since the first lane became due
@@ -931,6 +933,7 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
     while (true) {
         if (!alive && sp > 0) {   // resume a suspended particle
             p = lstack[--sp];
+            if (Adj) el = elstack[sp];
             alive = true;
             s.state = 0;
             s.nsteps = 0;
@@ -1058,7 +1061,15 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                             costhe = dsqrt(dmin((Real)1, dcosth));
                             rotate(a, b, c, sinthe, costhe, az, d.u, d.v, d.w);
                             d.E = pese2; d.iq = -1;
-                            if (!Adj && d.E > T.ecut && sp < LSTACK) { lstack[sp++] = p; p = d; }
+                            if (d.E > T.ecut && sp < LSTACK) {
+                                lstack[sp] = p;
+                                if (Adj) {
+                                    elstack[sp] = el;
+                                    for (int i = 0; i < el.n; ++i) el.k[i] = 0;
+                                }
+                                ++sp;
+                                p = d;
+                            }
                             else push_charged(P, P.eout, P.pout, d, acc, npush, edep_tot, err);
                             s.state = 0;
                             continue;
@@ -1100,7 +1111,15 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                                 costhe = dsqrt(dmin((Real)1, dcosth));
                                 rotate(a, b, c, sinthe, costhe, az, d.u, d.v, d.w);
                                 d.E = pese2; d.iq = iq_new;
-                                if (!Adj && d.E > T.ecut && sp < LSTACK) { lstack[sp++] = p; p = d; }
+                                if (d.E > T.ecut && sp < LSTACK) {
+                                lstack[sp] = p;
+                                if (Adj) {
+                                    elstack[sp] = el;
+                                    for (int i = 0; i < el.n; ++i) el.k[i] = 0;
+                                }
+                                ++sp;
+                                p = d;
+                            }
                                 else push_charged(P, P.eout, P.pout, d, acc, npush, edep_tot, err);
                                 s.state = 0;
                                 continue;

@@ -1,0 +1,161 @@
+"""The egs++ input driver (egs_gpu_app) against the Python binding of the same C ABI.
+
+The driver reads an egs++ input file (run control, EGS_XYZGeometry with
+`set medium`, parallel-beam or phase-space source, transport parameters, rng
+seeds) and writes a .3ddose file; the same problem set up through the Python
+binding must give the same dose (both are FP32 runs of the same histories;
+the file holds single-precision values).
+"""
+import gzip
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import egsnrc_gb300 as eg
+from egsnrc_gb300 import formats
+from egsnrc_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+APP = os.path.join(os.path.dirname(HERE), "egsnrc_gb300", "egs_gpu_app")
+
+SLAB = """
+:start run control:
+    ncase = 40000
+    nbatch = 4
+:stop run control:
+:start geometry definition:
+    :start geometry:
+        name     = plate
+        library  = egs_ndgeometry
+        type     = EGS_XYZGeometry
+        x-planes = -5, 5
+        y-planes = -5, 5
+        z-slabs = 0, 0.5, 20
+        :start media input:
+            media = H2O521ICRU ICRPBONE521ICRU
+            set medium = 4 6 1
+        :stop media input:
+    :stop geometry:
+    simulation geometry = plate
+:stop geometry definition:
+:start source definition:
+    :start source:
+        name      = beam
+        library   = egs_parallel_beam
+        charge    = -1
+        direction = 0 0 1
+        :start spectrum:
+            type = monoenergetic
+            energy = 12
+        :stop spectrum:
+        :start shape:
+            type     = point
+            position = 0 0 -8
+        :stop shape:
+    :stop source:
+    simulation source = beam
+:stop source definition:
+:start MC transport parameter:
+    Global ECUT = 0.7
+    Global PCUT = 0.01
+:stop MC transport parameter:
+:start rng definition:
+    initial seeds = 7 9
+:stop rng definition:
+"""
+
+PHSP = """
+:start run control:
+    ncase = 30000
+    nbatch = 3
+:stop run control:
+:start geometry definition:
+    :start geometry:
+        name     = box
+        library  = egs_ndgeometry
+        type     = EGS_XYZGeometry
+        x-slabs = -15, 2, 15
+        y-slabs = -15, 2, 15
+        z-slabs = 0, 2, 15
+        :start media input:
+            media = H2O521ICRU
+        :stop media input:
+    :stop geometry:
+    simulation geometry = box
+:stop geometry definition:
+:start source definition:
+    :start source:
+        name      = linac
+        library   = egs_phsp_source
+        phase space file = PHSPFILE
+        particle type = all
+        recycle photons = 1
+        recycle electrons = 1
+    :stop source:
+    :start source:
+        name      = moved
+        library   = egs_transformed_source
+        source name = linac
+        :start transformation:
+            translation = 0 0 -0.5
+        :stop transformation:
+    :stop source:
+    simulation source = moved
+:stop source definition:
+:start MC transport parameter:
+    Global ECUT = 0.7
+    Global PCUT = 0.01
+:stop MC transport parameter:
+:start rng definition:
+    initial seeds = 3
+:stop rng definition:
+"""
+
+
+def run_app(tmp_path, text, name):
+    f = tmp_path / (name + ".egsinp")
+    f.write_text(text)
+    r = subprocess.run([APP, "-i", str(f), "-p", "521icru", "-o", str(tmp_path / name)], capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    (nx, ny, nz), planes, dose, rel = formats.read_3ddose(str(tmp_path / (name + ".3ddose")))
+    return dose, rel
+
+
+def compare(dose_file, dose_py):
+    sel = dose_py > 1e-3 * dose_py.max()
+    assert sel.sum() > 5
+    assert np.allclose(dose_file[sel], dose_py[sel].astype(np.float32), rtol=2e-5)
+
+
+def test_app_slab_matches_binding(tmp_path):
+    dose_file, _ = run_app(tmp_path, SLAB, "slab")
+    zb = 0.5 * np.arange(21)          # z-slabs = 0, 0.5, 20: 20 slabs from 0 to 10 cm
+    med = np.zeros(len(zb) - 1, dtype=np.int32)
+    med[4:7] = 1                      # set medium = 4 6 1: regions 4..6 (0-based) are bone
+    g = eg.XYZGeometry([-5, 5], [-5, 5], zb, med)
+    eng = eg.DoseEngine([W.WATER, W.BONE], ecut=0.7, pcut=0.01)
+    eng.set_geometry(g)
+    eng.set_source(eg.ParallelBeam(charge=-1, energy=12.0, position=(0, 0, -8)))
+    eng.run(40000, nbatch=4, seed=7)
+    compare(dose_file, eng.dose()[0])
+
+
+def test_app_phase_space_source_matches_binding(tmp_path):
+    path = tmp_path / "EX16MVp.egsphsp1"
+    with gzip.open(os.path.join(HERE, "golden", "EX16MVp.egsphsp1.gz"), "rb") as a, open(path, "wb") as b:
+        shutil.copyfileobj(a, b)
+    dose_file, _ = run_app(tmp_path, PHSP.replace("PHSPFILE", str(path)), "phsp")
+    p, _ = formats.read_egsphsp(str(path))
+    b = -15 + 2.0 * np.arange(16)
+    g = eg.XYZGeometry(b, b, 2.0 * np.arange(16), 0)
+    eng = eg.DoseEngine([W.WATER], ecut=0.7, pcut=0.01)
+    eng.set_geometry(g)
+    eng.set_source(eg.PhaseSpaceSource(p, position=(0, 0, -0.5), recycle=1))
+    eng.run(30000, nbatch=3, seed=3)
+    compare(dose_file, eng.dose()[0])

@@ -18,8 +18,9 @@ template <class Real>
 struct Azim { Real c, s; };
 
 // $SELECT-AZIMUTHAL-ANGLE (src/egsnrc.macros:2491-2509)
+// out of line: see Rng::u (egs_device.cuh)
 template <class Real>
-__device__ inline Azim<Real> azimuth(Rng &r, int &err) {
+__device__ __noinline__ Azim<Real> azimuth(Rng &r, int &err) {
     Real xphi, xphi2, yphi, yphi2, rho2;
     int it = 0;
     do {

@@ -564,7 +564,7 @@ def main():
     bytes_k = steps_k * ALG_BYTES_PER_STEP + pushes_k * ALG_BYTES_PER_PUSH
     achieved = bytes_k / (ms_k / 1e3) / 1e9 if ms_k > 0 else None
     peak, peak_kind = measured_peak_hbm()
-    traffic = ncu_traffic("k_" + kern, wl["name"], steps_k / n_k)
+    traffic = ncu_traffic("k_" + kern, wl["name"] + ("-howfarless" if args.howfarless else ""), steps_k / n_k)
     roof = {"bound": "hbm", "kernel": "k_" + kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
             "traffic": traffic, "alg_bytes_per_launch": bytes_k / n_k, "launches": n_k,

@@ -97,6 +97,9 @@ struct Params {
 // for the next round to refill warps).
 constexpr unsigned REQUEUE_MIN = 32768;
 constexpr int LSTACK = 6;   // per-thread LIFO depth for charged secondaries
+// A photon lane crosses up to this many voxels per iteration of the persistent
+// loop before the warp's bookkeeping (refill, interaction batching) runs again.
+constexpr int PHOTON_HOPS = 8;
 constexpr int INTER_MAXWAIT = 24;   // longest wait of a lane due to interact
 
 // ------------------------------------------------------------- tallies ----
@@ -789,21 +792,24 @@ __global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
             s.state = 3;
             continue;
         }
-        int irnew = howfar(geom_of<Real, Multi>(P, p.pb), p.ir, p.x, p.y, p.z, p.u, p.v, p.w, ustep);
-        ++nstep;
-        if (Adj) gadd(P, ga, p.ir, -Gh * (ustep / gmfp) / s.rhor);
-        p.x += p.u * ustep; p.y += p.v * ustep; p.z += p.w * ustep;
-        s.dpmfp = dmax((Real)0, s.dpmfp - ustep / gmfp);
-        if (irnew != p.ir) {
-            p.ir = irnew;
-            if (irnew < 0) { esc_tot += (double)(p.E * p.wt); alive = false; continue; }
-            int mnew = G.med[irnew];
-            s.rhor = G.rhor[irnew];
-            if (mnew != s.medium) { s.medium = mnew; s.state = 1; continue; }
+#pragma unroll 1
+        for (int hop = 0;; ++hop) {
+            if (hop) { gmfp = s.gmfpr0 / s.rhor * s.cohfac; ustep = gmfp * s.dpmfp; }
+            int irnew = howfar(geom_of<Real, Multi>(P, p.pb), p.ir, p.x, p.y, p.z, p.u, p.v, p.w, ustep);
+            ++nstep;
+            if (Adj) gadd(P, ga, p.ir, -Gh * (ustep / gmfp) / s.rhor);
+            p.x += p.u * ustep; p.y += p.v * ustep; p.z += p.w * ustep;
+            s.dpmfp = dmax((Real)0, s.dpmfp - ustep / gmfp);
+            if (irnew != p.ir) {
+                p.ir = irnew;
+                if (irnew < 0) { esc_tot += (double)(p.E * p.wt); alive = false; break; }
+                int mnew = G.med[irnew];
+                s.rhor = G.rhor[irnew];
+                if (mnew != s.medium) { s.medium = mnew; s.state = 1; break; }
+            }
+            if (!(s.dpmfp > (Real)1e-8)) { s.state = 3; break; }
+            if (hop + 1 >= PHOTON_HOPS || ++s.nsteps > STEP_CAP) break;
         }
-        if (s.dpmfp > (Real)1e-8) continue;
-
-        s.state = 3;   // interaction due: wait for the warp's batch
     }
     acc_flush(P, acc);
     if (Adj) gflush(P, ga);

@@ -1944,7 +1944,7 @@ struct Engine : EngineBase {
         P.peak = (unsigned *)d_counts.p + 8;
         P.seed = seed;
         P.requeue_lanes = cfg.requeue_lanes > 0 ? cfg.requeue_lanes : 0;
-        P.inter_batch = cfg.inter_batch > 0 ? std::min(cfg.inter_batch, 32) : (cfg.inter_batch < 0 ? 1 : 12);
+        P.inter_batch = cfg.inter_batch > 0 ? std::min(cfg.inter_batch, 32) : (cfg.inter_batch < 0 ? 1 : 8);
         if (Multi) {
             P.probs = (const Geom<Real> *)d_probs.p; P.pseeds = (const uint32_t *)d_pseeds.p;
             P.psrc = (const Source *)d_psrc.p; P.pvoff = (const int *)d_pvoff.p;

@@ -52,7 +52,7 @@ typedef struct {
     int use_graph;        /* 1: replay the wavefront rounds from a CUDA graph (no
                              per-kernel timing); 0: direct launches with CUDA events */
     int inter_batch;      /* lanes of a warp due to interact before their interactions
-                             are sampled together; 0 = default (12), -1 = immediately
+                             are sampled together; 0 = default (8), -1 = immediately
                              (results are identical either way) */
     int howfarless;       /* 1: DOSXYZnrc HOWFARLESS transport (ihowfarless,
                              user_codes/dosxyznrc/dosxyznrc.mortran:425-455) for a

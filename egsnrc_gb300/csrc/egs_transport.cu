@@ -922,7 +922,6 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
     Particle<Real> lstack[LSTACK];
     int sp = 0;
     Acc<Real> acc{-1, 0u, (Real)0};
-    AccG<Real> ga{-1, (Real)0};
     EList<Real> el;
     el.n = 0;
     // adjoint: the voxel-visit lists of suspended particles; a secondary
@@ -1442,7 +1441,6 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
         }
     }
     acc_flush(P, acc);
-    if (Adj) gflush(P, ga);
     edep_tot += (double)edep_part;
     for (int o = 16; o > 0; o >>= 1) {
         nstep += __shfl_down_sync(0xffffffffu, nstep, o);

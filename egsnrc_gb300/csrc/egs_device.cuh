@@ -149,8 +149,15 @@ struct Rng {
     // Out of line (as is azimuth): the electron step loop is larger than the
     // instruction caches, and one shared copy of the draw for its ~30 call
     // sites measured 20-40% faster than inlined copies, even though the
-    // generator state then lives in local memory around each call.
-    __device__ __noinline__ float u() {
+    // generator state then lives in local memory around each call.  Sites that
+    // take two numbers in a row call u2 (one call instead of two: +3% on
+    // electron-dominated phantoms).
+    __device__ __noinline__ float u() { return draw(); }
+    __device__ __noinline__ float2 u2() {
+        float a = draw();
+        return make_float2(a, draw());
+    }
+    __device__ inline float draw() {
         uint32_t b = n >> 2;
         if (b != blk) {
             uint4 o = philox_block(b, (uint32_t)sid, (uint32_t)(sid >> 32), seed, hist);
@@ -166,6 +173,8 @@ struct Rng {
 // Uniform in (0,1) with 23 random bits: the same value in FP32 and FP64.
 template <class Real>
 __device__ inline Real urand(Rng &r) { return (Real)r.u(); }
+// two consecutive uniforms in one call (the same numbers as two urand calls)
+__device__ inline float2 urand2(Rng &r) { return r.u2(); }
 
 // --------------------------------------------------------- math shims ----
 // FP32 transport uses the SFU-based intrinsics; FP64 uses the full-precision

@@ -24,8 +24,9 @@ __device__ __noinline__ Azim<Real> azimuth(Rng &r, int &err) {
     Real xphi, xphi2, yphi, yphi2, rho2;
     int it = 0;
     do {
-        xphi = urand<Real>(r); xphi = 2 * xphi - 1; xphi2 = xphi * xphi;
-        yphi = urand<Real>(r); yphi2 = yphi * yphi;
+        float2 q = urand2(r);
+        xphi = (Real)q.x; xphi = 2 * xphi - 1; xphi2 = xphi * xphi;
+        yphi = (Real)q.y; yphi2 = yphi * yphi;
         rho2 = xphi2 + yphi2;
         if (++it > LOOP_CAP) { err = 1; break; }
     } while (rho2 > 1);

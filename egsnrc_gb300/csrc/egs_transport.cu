@@ -621,8 +621,12 @@ struct PhotonState {
 // history's weighted deposit G_h.
 // HFL: HOWFARLESS transport (one flight to the interaction or out of the
 // phantom; the voxel is located where the photon interacts).
+// FP32: eight CTAs per SM (at most 64 registers).  The photon loop is latency
+// bound and gains more from resident warps than it loses to its few spills
+// (+5% on slab phantoms over the unbounded 94-register build); the FP64 build
+// would spill ~1 KB per thread at that bound and keeps its registers.
 template <class Real, bool Multi, bool Adj = false, bool HFL = false>
-__global__ void __launch_bounds__(128) k_photon(Params<Real> P) {
+__global__ void __launch_bounds__(128, sizeof(Real) == 4 ? 8 : 1) k_photon(Params<Real> P) {
     const Tables<Real> &T = P.T;
     const Geom<Real> &G = P.G;
     const unsigned lane = threadIdx.x & 31u;
@@ -1043,10 +1047,11 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                             Real g2 = t0 * t0 / e02, g3 = (2 * t0 + 1) / e02, gmax = 1 + (Real)1.25 * g2, br, rejf4, r28;
                             int it = 0;
                             do {
-                                Real r27 = urand<Real>(p.rng);
+                                float2 q = urand2(p.rng);
+                                Real r27 = (Real)q.x;
                                 br = M2.te / (ekin - extrae * r27);
                                 Real rr2 = br / (1 - br);
-                                r28 = urand<Real>(p.rng);
+                                r28 = (Real)q.y;
                                 rejf4 = 1 + g2 * br * br + rr2 * (rr2 - g3);
                                 r28 = gmax * r28;
                                 if (++it > LOOP_CAP) { err = 1; break; }
@@ -1092,9 +1097,10 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                                 Real b4 = yp2 * yp, b3 = b4 + yp2, b2 = yp * (3 + y2), b1 = 2 - y2, br, rejf2, r04;
                                 int it = 0;
                                 do {
-                                    Real r03 = urand<Real>(p.rng);
+                                    float2 q = urand2(p.rng);
+                                    Real r03 = (Real)q.x;
                                     br = ep0 / (1 - ep0c * r03);
-                                    r04 = urand<Real>(p.rng);
+                                    r04 = (Real)q.y;
                                     rejf2 = (1 - beta2b * br * (b1 - br * (b2 - br * (b3 - br * b4))));
                                     if (++it > LOOP_CAP) { err = 1; break; }
                                 } while (!(r04 <= rejf2));
@@ -1135,9 +1141,10 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                             Real aa = p.u, bb = p.v, cc = p.w, ep, r02, rejf;
                             int it = 0;
                             do {
-                                Real r01 = urand<Real>(p.rng);
+                                float2 q = urand2(p.rng);
+                                Real r01 = (Real)q.x;
                                 ep = ep0 * dexp(r01 * wsamp);
-                                r02 = urand<Real>(p.rng);
+                                r02 = (Real)q.y;
                                 rejf = 1 - (ep * a - 1) * (ep * a - 1) / (ep * (a * a - 2));
                                 if (++it > LOOP_CAP) { err = 1; break; }
                             } while (!(r02 <= rejf));
@@ -1174,8 +1181,9 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                         Real esg, ese, r07, rejf;
                         int it = 0;
                         do {
-                            Real r06 = urand<Real>(p.rng);
-                            r07 = urand<Real>(p.rng);
+                            float2 q = urand2(p.rng);
+                            Real r06 = (Real)q.x;
+                            r07 = (Real)q.y;
                             Real br = brmin * dexp(r06 * waux);
                             esg = ekin * br;
                             ese = peie - esg;
@@ -1200,8 +1208,9 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                         Real rejmax = rjarg1 * rjarg3 - rjarg2, y2tst, rtest;
                         it = 0;
                         while (true) {
-                            y2tst = urand<Real>(p.rng);
-                            rtest = urand<Real>(p.rng);
+                            float2 q = urand2(p.rng);
+                            y2tst = (Real)q.x;
+                            rtest = (Real)q.y;
                             Real aux3 = z2maxi / (y2tst + (1 - y2tst) * z2maxi);
                             rtest = rtest * aux3 * rejmax;
                             y2tst = aux3 * aux3 - 1;
@@ -1812,8 +1821,8 @@ struct Engine : EngineBase {
     cudaEvent_t ev_in = nullptr;
     bool graph_ok = true;
 
-    cudaError_t enqueue_rounds(const Params<Real> &P0, int grid, int bs, bool events, bool multi, bool adj = false,
-                               bool hfl = false) {
+    cudaError_t enqueue_rounds(const Params<Real> &P0, int gp, int ge, int bs, bool events, bool multi,
+                               bool adj = false, bool hfl = false) {
         unsigned *counts = (unsigned *)d_counts.p;
         cudaError_t e = cudaSuccess;
         for (int r = 0; r < ROUNDS && e == cudaSuccess; ++r) {
@@ -1823,17 +1832,17 @@ struct Engine : EngineBase {
             if ((e = cudaMemsetAsync(counts + 2 * nxt, 0, 2 * sizeof(unsigned), ws))) break;
             if ((e = cudaMemsetAsync(counts + 4 + 2 * nxt, 0, 2 * sizeof(unsigned), ws))) break;
             if (events && (e = cudaEventRecord(gev[4 * r], ws))) break;
-            if (hfl) k_photon<Real, false, false, true><<<grid, bs, 0, ws>>>(P);
-            else if (adj) k_photon<Real, false, true><<<grid, bs, 0, ws>>>(P);
-            else if (multi) k_photon<Real, true><<<grid, bs, 0, ws>>>(P);
-            else k_photon<Real, false><<<grid, bs, 0, ws>>>(P);
+            if (hfl) k_photon<Real, false, false, true><<<gp, bs, 0, ws>>>(P);
+            else if (adj) k_photon<Real, false, true><<<gp, bs, 0, ws>>>(P);
+            else if (multi) k_photon<Real, true><<<gp, bs, 0, ws>>>(P);
+            else k_photon<Real, false><<<gp, bs, 0, ws>>>(P);
             if ((e = cudaGetLastError())) break;
             if (events && (e = cudaEventRecord(gev[4 * r + 1], ws))) break;
             if (events && (e = cudaEventRecord(gev[4 * r + 2], ws))) break;
-            if (hfl) k_electron<Real, false, false, true><<<grid, bs, 0, ws>>>(P);
-            else if (adj) k_electron<Real, false, true><<<grid, bs, 0, ws>>>(P);
-            else if (multi) k_electron<Real, true><<<grid, bs, 0, ws>>>(P);
-            else k_electron<Real, false><<<grid, bs, 0, ws>>>(P);
+            if (hfl) k_electron<Real, false, false, true><<<ge, bs, 0, ws>>>(P);
+            else if (adj) k_electron<Real, false, true><<<ge, bs, 0, ws>>>(P);
+            else if (multi) k_electron<Real, true><<<ge, bs, 0, ws>>>(P);
+            else k_electron<Real, false><<<ge, bs, 0, ws>>>(P);
             if ((e = cudaGetLastError())) break;
             if (events && (e = cudaEventRecord(gev[4 * r + 3], ws))) break;
         }
@@ -1842,14 +1851,14 @@ struct Engine : EngineBase {
 
     // Captures the rounds (without events) into a graph; on any failure the
     // engine keeps launching directly.
-    void build_graph(const Params<Real> &P0, int grid, int bs, bool multi, bool hfl) {
+    void build_graph(const Params<Real> &P0, int gp, int ge, int bs, bool multi, bool hfl) {
         if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
         if (cudaStreamBeginCapture(ws, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
             cudaGetLastError();
             graph_ok = false;
             return;
         }
-        cudaError_t e = enqueue_rounds(P0, grid, bs, false, multi, false, hfl);
+        cudaError_t e = enqueue_rounds(P0, gp, ge, bs, false, multi, false, hfl);
         cudaGraph_t g = nullptr;
         cudaError_t e2 = cudaStreamEndCapture(ws, &g);
         if (e == cudaSuccess && e2 == cudaSuccess && g) e = cudaGraphInstantiate(&gexec, g, 0);
@@ -1910,7 +1919,9 @@ struct Engine : EngineBase {
             chunk = tuned_chunk;
         }
         const int bs = cfg.block_size > 0 ? cfg.block_size : 128;
-        // persistent grids: never more CTAs than can be resident at once
+        // persistent grids, one per kernel: never more CTAs than can be
+        // resident at once (the photon kernel, with fewer registers, fits more
+        // CTAs per SM than the electron kernel)
         int occ_p = 1, occ_e = 1;
         const bool adj = mode && mode->adj;
         const bool hfl = cfg.howfarless > 0;
@@ -1927,8 +1938,9 @@ struct Engine : EngineBase {
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, Multi>, bs, 0));
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, Multi>, bs, 0));
         }
-        const int cps = std::max(1, std::min(cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm : 64, std::min(occ_p, occ_e)));
-        const int grid = sm_count * cps;
+        const int cps_cap = cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm : 64;
+        const int gp = sm_count * std::max(1, std::min(cps_cap, occ_p));
+        const int ge = sm_count * std::max(1, std::min(cps_cap, occ_e));
         Params<Real> P;
         std::memset(&P, 0, sizeof(P));
         P.T = T; P.G = G;
@@ -1957,7 +1969,7 @@ struct Engine : EngineBase {
         }
         P.pin = q[0]; P.ein = q[2]; P.pout = q[0]; P.eout = q[2];
         const bool use_graph = cfg.use_graph > 0 && graph_ok && !mode;
-        if (use_graph) build_graph(P, grid, bs, Multi, hfl);
+        if (use_graph) build_graph(P, gp, ge, bs, Multi, hfl);
         const bool graph = use_graph && gexec;
         unsigned *counts = (unsigned *)d_counts.p;
         CK(cudaEventRecord(ev_in, st));
@@ -1994,7 +2006,7 @@ struct Engine : EngineBase {
                 bool done = false;
                 for (int rep = 0; rep < 100000 / ROUNDS && !done; ++rep) {
                     if (graph) CK(cudaGraphLaunch(gexec, ws));
-                    else CK(enqueue_rounds(P, grid, bs, true, Multi, adj, hfl));
+                    else CK(enqueue_rounds(P, gp, ge, bs, true, Multi, adj, hfl));
                     CK(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, ws));
                     CK(cudaStreamSynchronize(ws));
                     if (rep == 0) { prof_ms[0] += elapsed(ev[0], ev[1]); ++prof_n[0]; }
@@ -2223,7 +2235,7 @@ struct Engine : EngineBase {
         int occ_p = 1, occ_e = 1;
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, false>, bs, 0));
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, false>, bs, 0));
-        const int grid = sm_count * std::max(1, std::min(occ_p, occ_e));
+        const int gp = sm_count * std::max(1, occ_p), ge = sm_count * std::max(1, occ_e);
         Params<Real> P;
         std::memset(&P, 0, sizeof(P));
         P.T = T; P.G = G;
@@ -2246,9 +2258,9 @@ struct Engine : EngineBase {
             CK(cudaMemsetAsync(counts + 2 * nxt, 0, 2 * sizeof(unsigned), st));
             CK(cudaMemsetAsync(counts + 4 + 2 * nxt, 0, 2 * sizeof(unsigned), st));
             P.pin = Q[cur]; P.ein = Q[2 + cur]; P.pout = Q[nxt]; P.eout = Q[2 + nxt];
-            k_photon<Real, false><<<grid, bs, 0, st>>>(P);
+            k_photon<Real, false><<<gp, bs, 0, st>>>(P);
             CK(cudaGetLastError());
-            k_electron<Real, false><<<grid, bs, 0, st>>>(P);
+            k_electron<Real, false><<<ge, bs, 0, st>>>(P);
             CK(cudaGetLastError());
             unsigned h[9];
             CK(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, st));

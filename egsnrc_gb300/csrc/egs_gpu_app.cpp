@@ -169,6 +169,7 @@ int main(int argc, char **argv) {
         cfg.estepe = mc->num("ESTEPE", cfg.estepe);
         cfg.ximax = mc->num("XImax", cfg.ximax);
         cfg.skindepth = mc->num("Skin depth for BCA", cfg.skindepth);
+        cfg.smax = mc->num("Global Smax", cfg.smax);
         struct Fixed { const char *key, *value; } fixed[] = {
             {"Boundary crossing algorithm", "exact"}, {"Electron-step algorithm", "presta-ii"},
             {"Spin effects", "off"}, {"Brems angular sampling", "km"}, {"Brems cross sections", "bh"},

@@ -1537,7 +1537,8 @@ struct PhantomDesc {
 
 struct EngineBase {
     virtual ~EngineBase() {}
-    virtual int load(const egs::Hatch &H, double ecut, double pcut, double skindepth, std::string &err) = 0;
+    virtual int load(const egs::Hatch &H, double ecut, double pcut, double skindepth, double smax,
+                     std::string &err) = 0;
     virtual int geometry(int nx, int ny, int nz, const double *xb, const double *yb, const double *zb,
                          const int32_t *med, const double *rhor, std::string &err) = 0;
     virtual int run(const Source &S, long long first, long long n, int nbatch, uint32_t seed, cudaStream_t st,
@@ -1604,7 +1605,8 @@ struct Engine : EngineBase {
         }
     }
 
-    int load(const egs::Hatch &H, double ecut, double pcut, double skindepth, std::string &err) override {
+    int load(const egs::Hatch &H, double ecut, double pcut, double skindepth, double smax,
+             std::string &err) override {
         nmed = (int)H.media.size();
         if (nmed > MAXMED) { err = "too many media"; return EGSGPU_ERR_ARG; }
         std::vector<Real> etab, gtab, pmax, ray, shell, elem, ms;
@@ -1702,7 +1704,7 @@ struct Engine : EngineBase {
         T.ms = (const Real *)d_ms.p; T.ms_i = (const int *)d_msi.p;
         T.dllambi = (Real)H.dllambi; T.dqmsi = (Real)H.dqmsi;
         T.nmed = nmed;
-        T.ecut = (Real)ecut; T.pcut = (Real)pcut; T.skindepth = (Real)skindepth; T.smaxir = (Real)1e10;
+        T.ecut = (Real)ecut; T.pcut = (Real)pcut; T.skindepth = (Real)skindepth; T.smaxir = (Real)smax;
         // tallies that do not depend on the geometry
         CK(d_energy.alloc(2 * sizeof(double)));
         CK(d_counters.alloc(CNT_N * sizeof(unsigned long long)));
@@ -2360,6 +2362,7 @@ int egsgpu_load_media(egsgpu_handle *h, const char *data_dir, const char *pegs_f
     egs::TransportParams tp;
     tp.ecut = h->cfg.ecut; tp.pcut = h->cfg.pcut;
     tp.estepe = h->cfg.estepe; tp.ximax = h->cfg.ximax; tp.skindepth_for_bca = h->cfg.skindepth;
+    if (h->cfg.smax > 0) tp.smaxir = h->cfg.smax;
     std::vector<std::string> nm;
     for (int i = 0; i < n; ++i) nm.push_back(names[i]);
     int rc = egs::hatch(data_dir, pegs_file, nm, tp, h->H, h->err);
@@ -2374,7 +2377,7 @@ int egsgpu_load_media(egsgpu_handle *h, const char *data_dir, const char *pegs_f
         return EGSGPU_ERR_ARG;
     }
     h->ecut = ecut; h->pcut = pcut;
-    rc = h->eng->load(h->H, ecut, pcut, h->cfg.skindepth, h->err);
+    rc = h->eng->load(h->H, ecut, pcut, h->cfg.skindepth, tp.smaxir, h->err);
     if (rc) return rc;
     h->have_media = true;
     return 0;

@@ -1,7 +1,8 @@
 """Stage the EGSnrc cross-section data files this engine reads into this folder.
 
 The transport engine reads the same data files as EGSnrc's HATCH step: the
-PEGS4 material file (``pegs4/data/521icru.pegs4dat``), the screened-Rutherford
+PEGS4 material files (``pegs4/data/521icru.pegs4dat``; ``700icru.pegs4dat``,
+the AE = 0.700 MeV media of the BEAMnrc examples), the screened-Rutherford
 multiple-scattering surface (``data/msnew.data``), the XCOM photon cross
 sections (``data/xcom_{photo,pair,triplet,rayleigh}.data``), the bound-Compton
 correction (``data/compton_sigma.data``), the Compton-profile shell list
@@ -21,6 +22,7 @@ import sys
 
 FILES = [
     ("pegs4/data/521icru.pegs4dat", "521icru.pegs4dat"),
+    ("pegs4/data/700icru.pegs4dat", "700icru.pegs4dat"),
     ("pegs4/pgs4form.dat", "pgs4form.dat"),
     ("data/msnew.data", "msnew.data"),
     ("data/xcom_photo.data", "xcom_photo.data"),

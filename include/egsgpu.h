@@ -61,6 +61,10 @@ typedef struct {
                              hinge path, step limits floored at half the smallest
                              voxel size.  Refused for inhomogeneous phantoms, several
                              phantoms and the adjoint. */
+    double smax;          /* maximum charged-particle step (cm): egs++ "Global Smax"
+                             (egs++/egs_advanced_application.cpp:487), the smaxir
+                             limit on tmxs in ELECTR (src/egsnrc.mortran:1179);
+                             <= 0 = no limit (1e10 cm, src/egsnrc.macros:2269) */
 } egsgpu_config;
 
 /* Source: egs++ EGS_ParallelBeam (sources/egs_parallel_beam) with a point

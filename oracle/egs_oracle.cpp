@@ -151,7 +151,12 @@ struct Tally {
     std::vector<double> batch, sum, sum2;
     double dep = 0, esc = 0;
     double steps = 0, psteps = 0, esteps = 0, pushes = 0;
+    // optional record of every particle that leaves the phantom, ESC_REC
+    // doubles each: charge, kinetic energy, x, y, z, u, v, w, weight, history
+    bool log_esc = false;
+    std::vector<double> esc_log;
 };
+constexpr int ESC_REC = 10;
 
 struct Oracle;
 
@@ -218,7 +223,14 @@ inline void deposit(Run &R, const Particle &p, double edep) {
         score_hist(R, p, edep * p.wt);
     }
 }
-inline void escape(Run &R, const Particle &p, double e) { R.T->esc += e * p.wt; }
+inline void escape(Run &R, const Particle &p, double e) {
+    R.T->esc += e * p.wt;
+    if (R.T->log_esc) {
+        const double r[ESC_REC] = {(double)p.iq, p.iq == 0 ? p.E : p.E - RM, p.x, p.y, p.z, p.u, p.v, p.w, p.wt,
+                                   (double)p.hist};
+        R.T->esc_log.insert(R.T->esc_log.end(), r, r + ESC_REC);
+    }
+}
 
 // ----------------------------------------------------------- geometry ----
 int howfar(const Geometry &G, int ireg, const Particle &p, double &t) {   // egs_nd_geometry.h:963-1104
@@ -1655,7 +1667,7 @@ int oracle_run(oracle_handle *h, long long first, long long n, int nbatch, uint3
     for (int b = 0; b < nbatch; ++b) {
         long long b0 = first + b * per_batch, bn = (b == nbatch - 1) ? n - b * per_batch : per_batch;
         std::vector<Tally> tl(threads);
-        for (auto &t : tl) t.batch.assign(h->T.batch.size(), 0);
+        for (auto &t : tl) { t.batch.assign(h->T.batch.size(), 0); t.log_esc = h->T.log_esc; }
         std::vector<std::thread> th;
         long long per = bn / threads;
         for (int t = 0; t < threads; ++t) {
@@ -1671,6 +1683,7 @@ int oracle_run(oracle_handle *h, long long first, long long n, int nbatch, uint3
             h->T.sum2[i] += d * d;
         }
         for (auto &t : tl) {
+            h->T.esc_log.insert(h->T.esc_log.end(), t.esc_log.begin(), t.esc_log.end());
             h->T.dep += t.dep; h->T.esc += t.esc; h->T.steps += t.steps;
             h->T.psteps += t.psteps; h->T.esteps += t.esteps; h->T.pushes += t.pushes;
         }
@@ -1678,6 +1691,28 @@ int oracle_run(oracle_handle *h, long long first, long long n, int nbatch, uint3
     h->nhist += n;
     h->nbatch += nbatch;
     return errs.load() ? 6 : 0;
+}
+
+// Maximum charged-particle step in cm (smaxir, src/egsnrc.mortran:1179);
+// smax <= 0 restores the default (no limit).
+int oracle_set_smax(oracle_handle *h, double smax) {
+    h->O.H.params.smaxir = smax > 0 ? smax : 1e10;
+    return 0;
+}
+
+// Records every particle that leaves the phantom from now on (on != 0), or
+// stops recording; either way the record is cleared.
+int oracle_set_escape_log(oracle_handle *h, int on) {
+    h->T.log_esc = on != 0;
+    h->T.esc_log.clear();
+    return 0;
+}
+// Number of recorded escapes; copies up to `max` records (ESC_REC doubles
+// each, in history order) to out.
+long long oracle_get_escapes(oracle_handle *h, double *out, long long max) {
+    long long n = (long long)(h->T.esc_log.size() / ESC_REC);
+    if (out && max > 0) std::copy(h->T.esc_log.begin(), h->T.esc_log.begin() + std::min(n, max) * ESC_REC, out);
+    return n;
 }
 
 int oracle_set_history_tally(oracle_handle *h, long long first, long long n) {

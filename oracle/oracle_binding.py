@@ -29,6 +29,10 @@ def lib():
         L.oracle_set_geometry.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp, dp, dp, C.POINTER(C.c_int32), dp]
         L.oracle_set_source.argtypes = [vp, C.c_void_p]
         L.oracle_set_howfarless.argtypes = [vp, C.c_int]
+        L.oracle_set_smax.argtypes = [vp, C.c_double]
+        L.oracle_set_escape_log.argtypes = [vp, C.c_int]
+        L.oracle_get_escapes.restype = i64
+        L.oracle_get_escapes.argtypes = [vp, dp, i64]
         L.oracle_run.argtypes = [vp, i64, i64, C.c_int, C.c_uint32, C.c_int, C.c_int]
         L.oracle_set_history_tally.argtypes = [vp, i64, i64]
         L.oracle_get_history_tally.argtypes = [vp, dp]
@@ -50,10 +54,10 @@ def _dp(a):
 
 
 class Oracle:
-    def __init__(self, media, ecut=0.521, pcut=0.010):
+    def __init__(self, media, ecut=0.521, pcut=0.010, pegs_file=PEGS_FILE):
         L = lib()
         names = (C.c_char_p * len(media))(*[m.encode() for m in media])
-        h = L.oracle_create(DATA_DIR.encode(), PEGS_FILE.encode(), names, len(media), ecut, pcut)
+        h = L.oracle_create(DATA_DIR.encode(), pegs_file.encode(), names, len(media), ecut, pcut)
         if not h:
             raise RuntimeError("oracle: media load failed")
         self.h = C.c_void_p(h)
@@ -70,6 +74,23 @@ class Oracle:
     def set_howfarless(self, on=True):
         """DOSXYZnrc HOWFARLESS transport in the current (homogeneous) phantom."""
         assert self.L.oracle_set_howfarless(self.h, int(bool(on))) == 0
+
+    def set_smax(self, smax):
+        """Maximum charged-particle step in cm (<= 0: no limit)."""
+        assert self.L.oracle_set_smax(self.h, float(smax)) == 0
+
+    def set_escape_log(self, on=True):
+        """Record (or stop recording) every particle that leaves the phantom."""
+        assert self.L.oracle_set_escape_log(self.h, int(bool(on))) == 0
+
+    def escapes(self):
+        """The recorded escapes as an (n, 10) array: charge, kinetic energy,
+        x, y, z, u, v, w, weight, history."""
+        n = self.L.oracle_get_escapes(self.h, None, 0)
+        out = np.zeros((n, 10))
+        if n:
+            self.L.oracle_get_escapes(self.h, _dp(out), n)
+        return out
 
     def set_source(self, src):
         self.src = src

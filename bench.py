@@ -407,13 +407,18 @@ def bench_batched(args, ws, rank, local, dist):
     h2d = sum(p["geometry"].xb.nbytes + p["geometry"].yb.nbytes + p["geometry"].zb.nbytes + p["geometry"].med.nbytes
               + p["geometry"].rhor.nbytes for p in ps)
     nv_all = sum(p["geometry"].nvox for p in ps)
+
+    def e2e_step():
+        e2e_eng.set_phantoms(ps)
+        e2e_eng.run_phantoms(nbatch=1)
+        e2e_eng.tallies()
+    for _ in range(Wm):   # the same untimed warm-up as the device-timed leg
+        e2e_step()
     torch.cuda.synchronize()
     te0 = time.perf_counter()
     for _ in range(K):
         flush.zero_()
-        e2e_eng.set_phantoms(ps)
-        e2e_eng.run_phantoms(nbatch=1)
-        e2e_eng.tallies()
+        e2e_step()
     torch.cuda.synchronize()
     Te = time.perf_counter() - te0
     e2e_eng.close()
@@ -524,7 +529,7 @@ def main():
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     flush.zero_()   # loads torch's fill kernel before anything is timed
     torch.cuda.synchronize()
-    base = rank * (K + Wm + 2) * H     # disjoint history ranges per rank
+    base = rank * 2 * (K + Wm + 1) * H     # disjoint history ranges per rank (device-timed and e2e legs)
     first = base
     for _ in range(Wm):
         eng.run(H, nbatch=1, seed=wl["seed"], first=first)
@@ -584,16 +589,22 @@ def main():
     e2e_eng.set_source(wl["source"])
     h2d = g.xb.nbytes + g.yb.nbytes + g.zb.nbytes + g.med.nbytes + g.rhor.nbytes
     d2h = 2 * g.nvox * 8 + 8 * 8
+
+    def e2e_step(first):
+        e2e_eng.set_geometry(g)
+        e2e_eng.run(H, nbatch=1, seed=wl["seed"], first=first)
+        return e2e_eng.tallies()
+    for _ in range(Wm):   # the same untimed warm-up as the device-timed leg
+        e2e_step(first)
+        first += H
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     te0 = time.perf_counter()
     for _ in range(K):
         flush.zero_()
-        e2e_eng.set_geometry(g)
-        e2e_eng.run(H, nbatch=1, seed=wl["seed"], first=first)
+        ss, ss2, _ = e2e_step(first)
         first += H
-        ss, ss2, _ = e2e_eng.tallies()
     torch.cuda.synchronize()
     Te = time.perf_counter() - te0
     if dist:

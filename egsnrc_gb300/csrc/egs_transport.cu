@@ -1516,12 +1516,19 @@ static void set_divisors(Geom<Real> &g) {
 
 struct DevMem {
     void *p = nullptr;
-    size_t n = 0;
+    size_t n = 0;   // bytes allocated
     ~DevMem() { if (p) cudaFree(p); }
+    // Keeps the current allocation when it is large enough, so that a caller
+    // who uploads a phantom of the same size every step allocates nothing
+    // (cudaMalloc and cudaFree synchronise the device).
     cudaError_t alloc(size_t bytes) {
-        if (p) { cudaFree(p); p = nullptr; }
-        n = bytes;
-        return cudaMalloc(&p, bytes ? bytes : 16);
+        const size_t want = bytes ? bytes : 16;
+        if (p && want <= n) return cudaSuccess;
+        if (p) { cudaFree(p); p = nullptr; n = 0; }
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) n = want;
+        else p = nullptr;
+        return e;
     }
 };
 

@@ -290,7 +290,7 @@ class DoseEngine:
 
     def tallies(self):
         nv = self.geom.nvox if self.geom is not None else self._nvox_all
-        s, s2, t = np.zeros(nv), np.zeros(nv), np.zeros(8)
+        s, s2, t = np.empty(nv), np.empty(nv), np.zeros(8)   # every element is written
         self._check(self.L.egsgpu_get_tallies(self.h, _dp(s), _dp(s2), _dp(t)))
         return s, s2, t
 

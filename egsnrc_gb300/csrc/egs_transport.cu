@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -28,6 +29,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/egsgpu.h"
@@ -1508,6 +1510,37 @@ static void fast_divisor(uint32_t d, uint32_t &m, int &l) {
     while ((1ull << l) < d) ++l;
     m = (uint32_t)((((1ull << 32) * ((1ull << l) - d)) / d) + 1);
 }
+// Runs f(begin, end) over the index range [0, n), split over up to 16 host
+// threads; small ranges run on the calling thread.  Used for the per-voxel
+// host loops of the phantom uploads (tens of millions of voxels per step for
+// a caller that uploads its phantoms every time).
+template <class F>
+static void host_parallel(long long n, F f) {
+    unsigned t = std::min(16u, std::max(1u, std::thread::hardware_concurrency()));
+    if (n < (1LL << 20) || t == 1) { f(0LL, n); return; }
+    std::vector<std::thread> th;
+    const long long per = (n + t - 1) / t;
+    for (unsigned k = 0; k < t; ++k) {
+        const long long b = k * per, e = std::min(n, b + per);
+        if (b < e) th.emplace_back(f, b, e);
+    }
+    for (auto &x : th) x.join();
+}
+
+// Checks the medium indices and relative densities of nv voxels: 0, or 1 for
+// a medium index out of range, 2 for a density that is not positive and finite.
+static int check_voxels(long long nv, const int32_t *med, const double *rhor, int nmed) {
+    std::atomic<int> bad{0};
+    host_parallel(nv, [&](long long b, long long e) {
+        for (long long i = b; i < e; ++i) {
+            if (med[i] < 0 || med[i] >= nmed) { bad.fetch_or(1); return; }
+            if (!(rhor[i] > 0) || !std::isfinite(rhor[i])) { bad.fetch_or(2); return; }
+        }
+    });
+    const int v = bad.load();
+    return (v & 1) ? 1 : (v & 2) ? 2 : 0;
+}
+
 template <class Real>
 static void set_divisors(Geom<Real> &g) {
     fast_divisor((uint32_t)g.nx, g.mnx, g.lnx);
@@ -1751,15 +1784,21 @@ struct Engine : EngineBase {
                  const double *rhor, std::string &err) override {
         nprob = 0;
         nvox = (long long)nx * ny * nz;
-        homogeneous = true;
-        for (long long i = 1; i < nvox && homogeneous; ++i) homogeneous = med[i] == med[0] && rhor[i] == rhor[0];
+        std::atomic<bool> mixed{false};
+        host_parallel(nvox, [&](long long b, long long e) {
+            for (long long i = b; i < e && !mixed.load(std::memory_order_relaxed); ++i)
+                if (med[i] != med[0] || rhor[i] != rhor[0]) mixed.store(true);
+        });
+        homogeneous = !mixed.load();
         mindel = 1e30;
         for (int i = 0; i < nx; ++i) mindel = std::min(mindel, xb[i + 1] - xb[i]);
         for (int i = 0; i < ny; ++i) mindel = std::min(mindel, yb[i + 1] - yb[i]);
         for (int i = 0; i < nz; ++i) mindel = std::min(mindel, zb[i + 1] - zb[i]);
         std::vector<Real> x(xb, xb + nx + 1), y(yb, yb + ny + 1), z(zb, zb + nz + 1), r(nvox);
         std::vector<uint8_t> m(nvox);
-        for (long long i = 0; i < nvox; ++i) { m[i] = (uint8_t)med[i]; r[i] = (Real)rhor[i]; }
+        host_parallel(nvox, [&](long long b, long long e) {
+            for (long long i = b; i < e; ++i) { m[i] = (uint8_t)med[i]; r[i] = (Real)rhor[i]; }
+        });
         auto up = [&](DevMem &d, const void *src, size_t bytes) -> cudaError_t {
             cudaError_t e = d.alloc(bytes);
             if (e != cudaSuccess) return e;
@@ -2146,10 +2185,23 @@ struct Engine : EngineBase {
             x.insert(x.end(), d.xb, d.xb + d.nx + 1);
             y.insert(y.end(), d.yb, d.yb + d.ny + 1);
             z.insert(z.end(), d.zb, d.zb + d.nz + 1);
-            for (long long i = 0; i < nv; ++i) { m.push_back((uint8_t)d.med[i]); r.push_back((Real)d.rhor[i]); }
             tot += nv;
         }
         voff[n] = (int)tot;
+        // voxels of all phantoms end to end, converted over the global index
+        m.resize(tot);
+        r.resize(tot);
+        host_parallel(tot, [&](long long b, long long e) {
+            int k = (int)(std::upper_bound(voff.begin(), voff.begin() + n + 1, (int)b) - voff.begin()) - 1;
+            for (long long i = b; i < e;) {
+                while (i >= voff[k + 1]) ++k;
+                const long long stop = std::min(e, (long long)voff[k + 1]);
+                const int32_t *md = pd[k].med;
+                const double *rh = pd[k].rhor;
+                const long long o = voff[k];
+                for (; i < stop; ++i) { m[i] = (uint8_t)md[i - o]; r[i] = (Real)rh[i - o]; }
+            }
+        });
         auto up = [&](DevMem &dm, const void *p, size_t bytes) -> cudaError_t {
             cudaError_t e = dm.alloc(bytes);
             if (e != cudaSuccess) return e;
@@ -2409,9 +2461,9 @@ int egsgpu_set_xyz_geometry(egsgpu_handle *h, int nx, int ny, int nz, const doub
     for (int i = 0; i < ny; ++i) if (!(yb[i + 1] > yb[i])) { h->err = "y-planes not increasing"; return EGSGPU_ERR_ARG; }
     for (int i = 0; i < nz; ++i) if (!(zb[i + 1] > zb[i])) { h->err = "z-planes not increasing"; return EGSGPU_ERR_ARG; }
     int nmed = (int)h->H.media.size();
-    for (long long i = 0; i < nv; ++i) {
-        if (med[i] < 0 || med[i] >= nmed) { h->err = "voxel medium index out of range"; return EGSGPU_ERR_ARG; }
-        if (!(rhor[i] > 0) || !std::isfinite(rhor[i])) { h->err = "voxel relative density must be positive and finite"; return EGSGPU_ERR_ARG; }
+    if (int bad = check_voxels(nv, med, rhor, nmed)) {
+        h->err = bad == 1 ? "voxel medium index out of range" : "voxel relative density must be positive and finite";
+        return EGSGPU_ERR_ARG;
     }
     int rc = h->eng->geometry(nx, ny, nz, xb, yb, zb, med, rhor, h->err);
     if (rc) return rc;
@@ -2566,9 +2618,9 @@ int egsgpu_set_phantoms(egsgpu_handle *h, int n, const egsgpu_phantom *ph) {
         for (int i = 0; i < q.nx; ++i) if (!(q.xb[i + 1] > q.xb[i])) { h->err = "x-planes not increasing" + at; return EGSGPU_ERR_ARG; }
         for (int i = 0; i < q.ny; ++i) if (!(q.yb[i + 1] > q.yb[i])) { h->err = "y-planes not increasing" + at; return EGSGPU_ERR_ARG; }
         for (int i = 0; i < q.nz; ++i) if (!(q.zb[i + 1] > q.zb[i])) { h->err = "z-planes not increasing" + at; return EGSGPU_ERR_ARG; }
-        for (long long i = 0; i < nv; ++i) {
-            if (q.med[i] < 0 || q.med[i] >= nmed) { h->err = "voxel medium index out of range" + at; return EGSGPU_ERR_ARG; }
-            if (!(q.rhor[i] > 0) || !std::isfinite(q.rhor[i])) { h->err = "bad voxel relative density" + at; return EGSGPU_ERR_ARG; }
+        if (int bad = check_voxels(nv, q.med, q.rhor, nmed)) {
+            h->err = (bad == 1 ? "voxel medium index out of range" : "bad voxel relative density") + at;
+            return EGSGPU_ERR_ARG;
         }
         std::vector<double> e, w;
         std::vector<int> b;
@@ -2624,7 +2676,11 @@ int egsgpu_set_phantoms(egsgpu_handle *h, int n, const egsgpu_phantom *ph) {
         long long nv = (long long)q.nx * q.ny * q.nz;
         P.nx = q.nx; P.ny = q.ny; P.nz = q.nz;
         P.xb.assign(q.xb, q.xb + q.nx + 1); P.yb.assign(q.yb, q.yb + q.ny + 1); P.zb.assign(q.zb, q.zb + q.nz + 1);
-        P.med.assign(q.med, q.med + nv); P.rhor.assign(q.rhor, q.rhor + nv);
+        P.med.resize(nv); P.rhor.resize(nv);
+        host_parallel(nv, [&](long long b, long long e) {
+            std::copy(q.med + b, q.med + e, P.med.begin() + b);
+            std::copy(q.rhor + b, q.rhor + e, P.rhor.begin() + b);
+        });
         P.voff = voff; P.histories = q.histories; P.nhist = 0;
         voff += nv;
     }

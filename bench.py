@@ -198,6 +198,13 @@ def ncu_traffic(kernel, workload, steps_per_launch):
         return None
 
 
+def pinned_pair(n):
+    """Two float64 host arrays of n elements in page-locked memory: the
+    e2e legs read the tallies into these every step."""
+    import torch
+    return tuple(torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for _ in range(2))
+
+
 def sigma_eff(sum_, sum2, nb, frac=0.5):
     m = sum_ / nb
     var = np.maximum(sum2 / nb - m * m, 0) / max(nb - 1, 1)
@@ -407,11 +414,12 @@ def bench_batched(args, ws, rank, local, dist):
     h2d = sum(p["geometry"].xb.nbytes + p["geometry"].yb.nbytes + p["geometry"].zb.nbytes + p["geometry"].med.nbytes
               + p["geometry"].rhor.nbytes for p in ps)
     nv_all = sum(p["geometry"].nvox for p in ps)
+    host_out = pinned_pair(nv_all)   # the caller's tally buffers, pinned and reused every step
 
     def e2e_step():
         e2e_eng.set_phantoms(ps)
         e2e_eng.run_phantoms(nbatch=1)
-        e2e_eng.tallies()
+        e2e_eng.tallies(out=host_out)
     for _ in range(Wm):   # the same untimed warm-up as the device-timed leg
         e2e_step()
     torch.cuda.synchronize()
@@ -590,10 +598,12 @@ def main():
     h2d = g.xb.nbytes + g.yb.nbytes + g.zb.nbytes + g.med.nbytes + g.rhor.nbytes
     d2h = 2 * g.nvox * 8 + 8 * 8
 
+    host_out = pinned_pair(g.nvox)   # the caller's tally buffers, pinned and reused every step
+
     def e2e_step(first):
         e2e_eng.set_geometry(g)
         e2e_eng.run(H, nbatch=1, seed=wl["seed"], first=first)
-        return e2e_eng.tallies()
+        return e2e_eng.tallies(out=host_out)
     for _ in range(Wm):   # the same untimed warm-up as the device-timed leg
         e2e_step(first)
         first += H

@@ -288,9 +288,20 @@ class DoseEngine:
         off, nv, _ = self.phantom_info(k)
         return s[off:off + nv], s2[off:off + nv]
 
-    def tallies(self):
+    def tallies(self, out=None):
+        """(sum, sum2, totals) of the energy per voxel over batches (MeV).
+        `out`: an optional (sum, sum2) pair of contiguous float64 arrays of
+        nvox elements to fill, so that a caller reading the tallies every step
+        reuses its host memory, as a C caller of egsgpu_get_tallies does."""
         nv = self.geom.nvox if self.geom is not None else self._nvox_all
-        s, s2, t = np.empty(nv), np.empty(nv), np.zeros(8)   # every element is written
+        if out is None:
+            s, s2 = np.empty(nv), np.empty(nv)   # every element is written
+        else:
+            s, s2 = out
+            for a in (s, s2):
+                if a.dtype != np.float64 or a.size != nv or not a.flags.c_contiguous or not a.flags.writeable:
+                    raise ValueError("tallies(out=...) wants two writable contiguous float64 arrays of %d elements" % nv)
+        t = np.zeros(8)
         self._check(self.L.egsgpu_get_tallies(self.h, _dp(s), _dp(s2), _dp(t)))
         return s, s2, t
 

@@ -27,6 +27,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <new>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -1527,15 +1528,51 @@ static void host_parallel(long long n, F f) {
     for (auto &x : th) x.join();
 }
 
+// Calls f(k, begin, end) for the voxels [begin, end) of phantom k, over n
+// phantoms laid end to end (phantom k's voxels are [off[k], off[k+1]) of the
+// global range), split over host threads by the global range.
+template <class F>
+static void phantoms_parallel(const std::vector<long long> &off, F f) {
+    const int n = (int)off.size() - 1;
+    host_parallel(off[n], [&](long long b, long long e) {
+        int k = (int)(std::upper_bound(off.begin(), off.end(), b) - off.begin()) - 1;
+        for (long long i = b; i < e;) {
+            while (i >= off[k + 1]) ++k;
+            const long long stop = std::min(e, off[k + 1]);
+            f(k, i - off[k], stop - off[k]);
+            i = stop;
+        }
+    });
+}
+
+// An allocator whose resize() leaves new elements of trivial types
+// uninitialised: the voxel copies overwrite every element, and zero-filling
+// a gigabyte first costs more than the copy itself.
+template <class T>
+struct NoInitAlloc : std::allocator<T> {
+    template <class U> struct rebind { using other = NoInitAlloc<U>; };
+    NoInitAlloc() = default;
+    template <class U> NoInitAlloc(const NoInitAlloc<U> &) noexcept {}
+    template <class U> void construct(U *p) noexcept { ::new ((void *)p) U; }
+    template <class U, class... A> void construct(U *p, A &&...a) { ::new ((void *)p) U(std::forward<A>(a)...); }
+};
+template <class T>
+using raw_vector = std::vector<T, NoInitAlloc<T>>;
+
 // Checks the medium indices and relative densities of nv voxels: 0, or 1 for
 // a medium index out of range, 2 for a density that is not positive and finite.
+static int check_range(long long nv, const int32_t *med, const double *rhor, int nmed) {
+    for (long long i = 0; i < nv; ++i) {
+        if (med[i] < 0 || med[i] >= nmed) return 1;
+        if (!(rhor[i] > 0) || !std::isfinite(rhor[i])) return 2;
+    }
+    return 0;
+}
+// The same over host threads.
 static int check_voxels(long long nv, const int32_t *med, const double *rhor, int nmed) {
     std::atomic<int> bad{0};
     host_parallel(nv, [&](long long b, long long e) {
-        for (long long i = b; i < e; ++i) {
-            if (med[i] < 0 || med[i] >= nmed) { bad.fetch_or(1); return; }
-            if (!(rhor[i] > 0) || !std::isfinite(rhor[i])) { bad.fetch_or(2); return; }
-        }
+        if (int v = check_range(e - b, med + b, rhor + b, nmed)) bad.fetch_or(v);
     });
     const int v = bad.load();
     return (v & 1) ? 1 : (v & 2) ? 2 : 0;
@@ -1794,8 +1831,9 @@ struct Engine : EngineBase {
         for (int i = 0; i < nx; ++i) mindel = std::min(mindel, xb[i + 1] - xb[i]);
         for (int i = 0; i < ny; ++i) mindel = std::min(mindel, yb[i + 1] - yb[i]);
         for (int i = 0; i < nz; ++i) mindel = std::min(mindel, zb[i + 1] - zb[i]);
-        std::vector<Real> x(xb, xb + nx + 1), y(yb, yb + ny + 1), z(zb, zb + nz + 1), r(nvox);
-        std::vector<uint8_t> m(nvox);
+        std::vector<Real> x(xb, xb + nx + 1), y(yb, yb + ny + 1), z(zb, zb + nz + 1);
+        raw_vector<Real> r(nvox);
+        raw_vector<uint8_t> m(nvox);
         host_parallel(nvox, [&](long long b, long long e) {
             for (long long i = b; i < e; ++i) { m[i] = (uint8_t)med[i]; r[i] = (Real)rhor[i]; }
         });
@@ -2171,8 +2209,9 @@ struct Engine : EngineBase {
     DevMem d_probs, d_pseeds, d_psrc, d_pvoff, d_pprefix, d_pfirst;
 
     int problems(int n, const PhantomDesc *pd, const Source *src, std::string &err) override {
-        std::vector<Real> x, y, z, r;
-        std::vector<uint8_t> m;
+        std::vector<Real> x, y, z;
+        raw_vector<Real> r;
+        raw_vector<uint8_t> m;
         std::vector<int> voff(n + 1, 0);
         std::vector<long long> xo(n), yo(n), zo(n);
         long long tot = 0;
@@ -2191,16 +2230,11 @@ struct Engine : EngineBase {
         // voxels of all phantoms end to end, converted over the global index
         m.resize(tot);
         r.resize(tot);
-        host_parallel(tot, [&](long long b, long long e) {
-            int k = (int)(std::upper_bound(voff.begin(), voff.begin() + n + 1, (int)b) - voff.begin()) - 1;
-            for (long long i = b; i < e;) {
-                while (i >= voff[k + 1]) ++k;
-                const long long stop = std::min(e, (long long)voff[k + 1]);
-                const int32_t *md = pd[k].med;
-                const double *rh = pd[k].rhor;
-                const long long o = voff[k];
-                for (; i < stop; ++i) { m[i] = (uint8_t)md[i - o]; r[i] = (Real)rh[i - o]; }
-            }
+        const std::vector<long long> off(voff.begin(), voff.end());
+        phantoms_parallel(off, [&](int k, long long b, long long e) {
+            uint8_t *mo = m.data() + off[k];
+            Real *ro = r.data() + off[k];
+            for (long long i = b; i < e; ++i) { mo[i] = (uint8_t)pd[k].med[i]; ro[i] = (Real)pd[k].rhor[i]; }
         });
         auto up = [&](DevMem &dm, const void *p, size_t bytes) -> cudaError_t {
             cudaError_t e = dm.alloc(bytes);
@@ -2350,8 +2384,9 @@ struct egsgpu_handle {
     std::unique_ptr<EngineBase> eng;
     // geometry copies for dose normalisation
     int nx = 0, ny = 0, nz = 0;
-    std::vector<double> xb, yb, zb, rhor;
-    std::vector<int32_t> med;
+    std::vector<double> xb, yb, zb;
+    raw_vector<double> rhor;
+    raw_vector<int32_t> med;
     // source
     Source S{};
     DevMem d_edges, d_wi, d_bin, d_phsp;
@@ -2362,8 +2397,9 @@ struct egsgpu_handle {
     // normalisation, global voxel offsets, histories run per phantom
     struct Phantom {
         int nx, ny, nz;
-        std::vector<double> xb, yb, zb, rhor;
-        std::vector<int32_t> med;
+        std::vector<double> xb, yb, zb;
+        raw_vector<double> rhor;
+        raw_vector<int32_t> med;
         long long voff, histories, nhist;
     };
     std::vector<Phantom> phantoms;
@@ -2469,7 +2505,11 @@ int egsgpu_set_xyz_geometry(egsgpu_handle *h, int nx, int ny, int nz, const doub
     if (rc) return rc;
     h->nx = nx; h->ny = ny; h->nz = nz;
     h->xb.assign(xb, xb + nx + 1); h->yb.assign(yb, yb + ny + 1); h->zb.assign(zb, zb + nz + 1);
-    h->med.assign(med, med + nv); h->rhor.assign(rhor, rhor + nv);
+    h->med.resize(nv); h->rhor.resize(nv);
+    host_parallel(nv, [&](long long b, long long e) {
+        std::copy(med + b, med + e, h->med.begin() + b);
+        std::copy(rhor + b, rhor + e, h->rhor.begin() + b);
+    });
     h->have_geom = true;
     h->phantoms.clear();
     h->nhist = 0; h->nbatch = 0;
@@ -2618,10 +2658,6 @@ int egsgpu_set_phantoms(egsgpu_handle *h, int n, const egsgpu_phantom *ph) {
         for (int i = 0; i < q.nx; ++i) if (!(q.xb[i + 1] > q.xb[i])) { h->err = "x-planes not increasing" + at; return EGSGPU_ERR_ARG; }
         for (int i = 0; i < q.ny; ++i) if (!(q.yb[i + 1] > q.yb[i])) { h->err = "y-planes not increasing" + at; return EGSGPU_ERR_ARG; }
         for (int i = 0; i < q.nz; ++i) if (!(q.zb[i + 1] > q.zb[i])) { h->err = "z-planes not increasing" + at; return EGSGPU_ERR_ARG; }
-        if (int bad = check_voxels(nv, q.med, q.rhor, nmed)) {
-            h->err = (bad == 1 ? "voxel medium index out of range" : "bad voxel relative density") + at;
-            return EGSGPU_ERR_ARG;
-        }
         std::vector<double> e, w;
         std::vector<int> b;
         if (int rc = build_source(&q.source, src[k], e, w, b, h->err)) { h->err += at; return rc; }
@@ -2642,6 +2678,20 @@ int egsgpu_set_phantoms(egsgpu_handle *h, int n, const egsgpu_phantom *ph) {
         if (src[k].charge != 0) smax.charge = -1;
         pd[k] = PhantomDesc{q.nx, q.ny, q.nz, q.xb, q.yb, q.zb, q.med, q.rhor, q.seed, q.histories};
     }
+    // the voxels of all phantoms, checked in one pass over host threads
+    std::vector<long long> off(n + 1, 0);
+    for (int k = 0; k < n; ++k) off[k + 1] = off[k] + (long long)ph[k].nx * ph[k].ny * ph[k].nz;
+    std::vector<std::atomic<int>> bad(n);
+    for (auto &b : bad) b.store(0);
+    phantoms_parallel(off, [&](int k, long long b, long long e) {
+        if (int v = check_range(e - b, ph[k].med + b, ph[k].rhor + b, nmed)) bad[k].fetch_or(v);
+    });
+    for (int k = 0; k < n; ++k)
+        if (int v = bad[k].load()) {
+            h->err = std::string((v & 1) ? "voxel medium index out of range" : "bad voxel relative density") +
+                     " (phantom " + std::to_string(k) + ")";
+            return EGSGPU_ERR_ARG;
+        }
     std::string &err = h->err;
     if (nphsp_all > 0) {
         CK(h->d_pphsp.alloc((size_t)nphsp_all * 7 * sizeof(float)));
@@ -2668,23 +2718,25 @@ int egsgpu_set_phantoms(egsgpu_handle *h, int n, const egsgpu_phantom *ph) {
     }
     int rc = h->eng->problems(n, pd.data(), src.data(), h->err);
     if (rc) { h->phantoms.clear(); h->have_geom = false; return rc; }
-    h->phantoms.assign(n, egsgpu_handle::Phantom{});
-    long long voff = 0;
+    // host copies for the dose normalisation; the phantoms of the previous
+    // call keep their storage, so a caller who uploads the same phantoms every
+    // step reallocates nothing
+    h->phantoms.resize(n);
     for (int k = 0; k < n; ++k) {
         const egsgpu_phantom &q = ph[k];
         egsgpu_handle::Phantom &P = h->phantoms[k];
-        long long nv = (long long)q.nx * q.ny * q.nz;
+        const long long nv = off[k + 1] - off[k];
         P.nx = q.nx; P.ny = q.ny; P.nz = q.nz;
         P.xb.assign(q.xb, q.xb + q.nx + 1); P.yb.assign(q.yb, q.yb + q.ny + 1); P.zb.assign(q.zb, q.zb + q.nz + 1);
         P.med.resize(nv); P.rhor.resize(nv);
-        host_parallel(nv, [&](long long b, long long e) {
-            std::copy(q.med + b, q.med + e, P.med.begin() + b);
-            std::copy(q.rhor + b, q.rhor + e, P.rhor.begin() + b);
-        });
-        P.voff = voff; P.histories = q.histories; P.nhist = 0;
-        voff += nv;
+        P.voff = off[k]; P.histories = q.histories; P.nhist = 0;
     }
-    h->mvox = voff;
+    phantoms_parallel(off, [&](int k, long long b, long long e) {
+        egsgpu_handle::Phantom &P = h->phantoms[k];
+        std::copy(ph[k].med + b, ph[k].med + e, P.med.begin() + b);
+        std::copy(ph[k].rhor + b, ph[k].rhor + e, P.rhor.begin() + b);
+    });
+    h->mvox = off[n];
     h->Smax = smax;
     h->have_geom = true;
     h->have_source = true;

@@ -8,7 +8,8 @@
   * a phantom of more than 2^24 voxels with dimensions that are not powers
     of two, which exercises the multiply-high voxel decoding far from zero;
   * rejected geometries (planes not increasing, medium out of range,
-    non-positive density) and run ranges.
+    non-positive density) and run ranges;
+  * tallies read into the caller's buffers.
 """
 import numpy as np
 import pytest
@@ -163,4 +164,20 @@ def test_rejected_geometries_and_ranges():
     for kw in (dict(n=-1, nbatch=1), dict(n=10, nbatch=0)):
         with pytest.raises(eg.EGSError):
             e.run(kw["n"], nbatch=kw["nbatch"], seed=1)
+    e.close()
+
+
+def test_tallies_into_caller_buffers():
+    g = W.centred_geometry(12, 0.5)
+    e, _ = pair(g, eg.ParallelBeam(charge=-1, energy=3.0, position=(0, 0, -1)))
+    e.run(2000, nbatch=4, seed=3)
+    s, s2, t = e.tallies()
+    out = (np.full(g.nvox, np.nan), np.full(g.nvox, np.nan))
+    s_b, s2_b, t_b = e.tallies(out=out)
+    assert s_b is out[0] and s2_b is out[1]
+    assert np.array_equal(s, s_b) and np.array_equal(s2, s2_b) and np.array_equal(t, t_b)
+    for bad in ((np.empty(g.nvox - 1), np.empty(g.nvox)), (np.empty(g.nvox, np.float32), np.empty(g.nvox)),
+                (np.empty(2 * g.nvox)[::2], np.empty(g.nvox))):
+        with pytest.raises(ValueError):
+            e.tallies(out=bad)
     e.close()

@@ -33,7 +33,7 @@ class Config(C.Structure):
                 ("skindepth", C.c_double), ("precision", C.c_int), ("block_size", C.c_int),
                 ("ctas_per_sm", C.c_int), ("chunk", C.c_longlong), ("capacity", C.c_longlong),
                 ("requeue_lanes", C.c_int), ("use_graph", C.c_int), ("inter_batch", C.c_int),
-                ("howfarless", C.c_int), ("smax", C.c_double)]
+                ("howfarless", C.c_int), ("smax", C.c_double), ("bca_algorithm", C.c_int)]
 
 
 class SourceStruct(C.Structure):

@@ -170,8 +170,15 @@ int main(int argc, char **argv) {
         cfg.ximax = mc->num("XImax", cfg.ximax);
         cfg.skindepth = mc->num("Skin depth for BCA", cfg.skindepth);
         cfg.smax = mc->num("Global Smax", cfg.smax);
+        if (mc->has("Boundary crossing algorithm")) {
+            const std::string b = egsin::norm(mc->get("Boundary crossing algorithm"));
+            if (b == "presta-i") cfg.bca_algorithm = 1;
+            else if (b != "exact")
+                return fail("'Boundary crossing algorithm = " + mc->get("Boundary crossing algorithm") +
+                            "' is not supported (EXACT or PRESTA-I)");
+        }
         struct Fixed { const char *key, *value; } fixed[] = {
-            {"Boundary crossing algorithm", "exact"}, {"Electron-step algorithm", "presta-ii"},
+            {"Electron-step algorithm", "presta-ii"},
             {"Spin effects", "off"}, {"Brems angular sampling", "km"}, {"Brems cross sections", "bh"},
             {"Pair angular sampling", "simple"}, {"Pair cross sections", "bh"}, {"Triplet production", "off"},
             {"Electron impact ionization", "off"}, {"Photonuclear attenuation", "off"},

@@ -520,6 +520,22 @@ int hatch(const std::string &dir, const std::string &pegs_file, const std::vecto
         H.dllambi = 1. / ((llammax - llammin) / (MS_NL - 1));
         H.dqmsi = 1. / (QMAX_MS / (MS_NQ - 1));
     }
+    // PRESTA-I boundary crossing without a skin depth given: the old PRESTA
+    // default minimum step, from the lowest ECUT and blcc, xcc as read from
+    // PEGS4 (before the conversion below), in elastic MFPs
+    // (src/egsnrc.mortran:2794-2815)
+    if (!H.params.exact_bca && H.params.skindepth_for_bca <= 1e-4) {
+        double ecutmn = 1e30;
+        for (auto &m : H.media) ecutmn = std::min(ecutmn, std::max(H.params.ecut, m.ae));
+        double tstbmn = 1e30;
+        for (auto &m : H.media) {
+            double t = (ecutmn - RM) * (ecutmn + RM) / (ecutmn * ecutmn);
+            t = m.blcc * t * (ecutmn / m.xcc) * (ecutmn / m.xcc);
+            const double aux = std::log(t);
+            tstbmn = std::min(tstbmn, std::log(t / aux));
+        }
+        H.params.skindepth_for_bca = std::exp(tstbmn);
+    }
     for (auto &m : H.media) {
         m.blcc = 1.16699413758864573 * m.blcc;
         m.xcc = m.xcc * m.xcc;

@@ -90,8 +90,9 @@ struct Medium {
 struct TransportParams {
     double ecut = 0.521, pcut = 0.010;        // total energy for e-, MeV
     double estepe = 0.25, ximax = 0.5;       // egsnrc.macros:2265, :2260
-    double skindepth_for_bca = 3.0;          // egsnrc.macros:2256
-    bool exact_bca = true;                   // BCA = EXACT
+    double skindepth_for_bca = 3.0;          // egsnrc.macros:2256; PRESTA-I with <= 1e-4: the
+                                             // old PRESTA default, set by hatch()
+    bool exact_bca = true;                   // BCA: EXACT, or PRESTA-I (false)
     int transport_algorithm = 0;             // 0 = PRESTA-II
     bool spin_effects = false;               // spinms.data absent
     int ibcmp = 3;                           // bound Compton norej

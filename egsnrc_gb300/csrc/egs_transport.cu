@@ -912,7 +912,13 @@ __device__ inline Real eloss_g(const Tables<Real> &T, const MedScalars<Real> &M,
 
 // Adj: adjoint replay of the continuous energy loss (see EList).
 // HFL: HOWFARLESS transport with hinge dose deposition (hfl_hinge).
-template <class Real, bool Multi, bool Adj = false, bool HFL = false>
+// PI: PRESTA-I boundary crossing instead of EXACT (src/egsnrc.mortran:1247-1345):
+// every step within tperp is a PRESTA-II step; a step that reaches past the
+// nearest boundary is shortened by the average path-length correction
+// ($SET-USTEP), corrected back if howfar cuts it ($SET-TVSTEP), and deflected
+// once at its end by mscat.  Its own instantiation, so that the EXACT kernels
+// carry none of this code.
+template <class Real, bool Multi, bool Adj = false, bool HFL = false, bool PI = false>
 __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
     const Tables<Real> &T = P.T;
     const Geom<Real> &G = P.G;
@@ -1314,14 +1320,31 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
             Real p2 = s.eke * (s.eke + 2 * rm), beta2 = p2 / (p2 + rm * rm);
             Real ssmfp = beta2 / blccl, skindepth = T.skindepth * ssmfp;
             tustep = dmin(tustep, dmax(tperp, skindepth));
-            bool callhowfar, dosingle = false, callmsdist;
+            bool callhowfar, dosingle = false, callmsdist, domultiple = false;
             Real ustep, uf, vf, wf, xf, yf, zf;
             Real de = 0;
+            // PRESTA-I: the multiple-scattering parameters of the step
+            // ($CALCULATE-XI, src/egsnrc.macros:1323-1348; spin effects off)
+            Real ms_beta2 = 0, ms_chia2 = 0, ms_xi = 0;
+            auto calculate_xi = [&](Real ekems, Real len) {
+                const Real pq2 = ekems * (ekems + 2 * rm), xccl = rhof * M.xcc;
+                ms_beta2 = pq2 / (pq2 + rm * rm);
+                ms_chia2 = xccl / (4 * blccl * pq2);
+                ms_xi = (Real)0.5 * xccl / pq2 / ms_beta2 * len;
+                ms_xi = ms_xi * (dlog(1 + 1 / ms_chia2) - 1 / (1 + ms_chia2));
+            };
             ++nstep;
-            if (tustep <= tperp && tustep > skindepth) {
+            if (tustep <= tperp && (PI || tustep > skindepth)) {
                 callhowfar = false;
                 callmsdist = true;
                 ustep = tustep;
+            } else if (PI) {   // $SET-USTEP (src/egsnrc.macros:1308-1321)
+                callmsdist = false;
+                domultiple = true;
+                calculate_xi(s.eke - (Real)0.5 * tustep * dedx, tustep);
+                ustep = ms_xi < (Real)0.1 ? tustep * (1 - ms_xi * ((Real)0.5 - ms_xi * (Real)0.166667))
+                                          : tustep * (1 - dexp(-ms_xi)) / ms_xi;
+                callhowfar = !(ustep < tperp);
             } else {
                 callmsdist = false;
                 Real rnnoss = urand<Real>(p.rng);
@@ -1341,6 +1364,7 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                 ustep = tustep;
                 callhowfar = !(ustep < tperp);
             }
+            const Real ustep0 = ustep;
             int irold = p.ir, irnew = p.ir, axis = -1;
             if (callhowfar) irnew = HFL ? hfl_howfar(GP, p, ustep) : howfar(GP, p.ir, p.x, p.y, p.z, p.u, p.v, p.w, ustep, axis);
             if (Adj && irnew != irold && axis >= 0) {   // the step ends on a voxel face
@@ -1367,7 +1391,15 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
             }
             if (!ecut_discard) {
                 Real vstep = ustep, tvstep = callhowfar ? vstep : tustep;
-                if (callhowfar && tvstep != tustep) dosingle = false;
+                if (PI && callhowfar) {   // $SET-TVSTEP (src/egsnrc.macros:1350-1392)
+                    if (vstep < ustep0) {
+                        calculate_xi(s.eke - (Real)0.5 * tustep * vstep / ustep0 * dedx, vstep);
+                        if (ms_xi < (Real)0.1) tvstep = vstep * (1 + ms_xi * ((Real)0.5 + ms_xi * (Real)0.333333));
+                        else if (ms_xi < (Real)0.999999) tvstep = -vstep * dlog(1 - ms_xi) / ms_xi;
+                        else { err = 1; alive = false; continue; }
+                    } else tvstep = tustep;
+                }
+                if (!PI && callhowfar && tvstep != tustep) dosingle = false;
                 de = eloss_g(T, M, qel, (Real)tvstep, (Real)s.eke, (Real)s.elke, s.lelke, range, (Real)rhof);
                 if (callmsdist) msdist_pII(T, M, p, s.eke, (Real)de, tustep, rhof, uf, vf, wf, xf, yf, zf, err);
                 Real edep = (Real)de, ekef = s.eke - edep;
@@ -1380,6 +1412,14 @@ __global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
                         Real xi = urand<Real>(p.rng);
                         xi = 2 * chia2 * xi / (1 - xi + chia2);
                         Real costhe = 1 - xi, sinthe = dsqrt(xi * (2 - xi));
+                        Azim<Real> az = azimuth<Real>(p.rng, err);
+                        rotate(p.u, p.v, p.w, sinthe, costhe, az, uf, vf, wf);
+                    } else if (PI && domultiple) {   // src/egsnrc.mortran:1480-1496, 1561-1567
+                        const Real lambda = blccl * tvstep / ms_beta2 / (1 + ms_chia2);
+                        MsState<Real> st;
+                        st.find_index = true; st.i = 0; st.j = 0; st.omega2 = 0;
+                        Real costhe, sinthe;
+                        mscat(T, p.rng, lambda, ms_chia2, ms_xi, st, costhe, sinthe, err);
                         Azim<Real> az = azimuth<Real>(p.rng, err);
                         rotate(p.u, p.v, p.w, sinthe, costhe, az, uf, vf, wf);
                     } else { uf = p.u; vf = p.v; wf = p.w; }
@@ -1909,6 +1949,7 @@ struct Engine : EngineBase {
 
     cudaError_t enqueue_rounds(const Params<Real> &P0, int gp, int ge, int bs, bool events, bool multi,
                                bool adj = false, bool hfl = false) {
+        const bool pi = cfg.bca_algorithm == 1;
         unsigned *counts = (unsigned *)d_counts.p;
         cudaError_t e = cudaSuccess;
         for (int r = 0; r < ROUNDS && e == cudaSuccess; ++r) {
@@ -1926,6 +1967,7 @@ struct Engine : EngineBase {
             if (events && (e = cudaEventRecord(gev[4 * r + 1], ws))) break;
             if (events && (e = cudaEventRecord(gev[4 * r + 2], ws))) break;
             if (hfl) k_electron<Real, false, false, true><<<ge, bs, 0, ws>>>(P);
+            else if (pi) k_electron<Real, false, false, false, true><<<ge, bs, 0, ws>>>(P);
             else if (adj) k_electron<Real, false, true><<<ge, bs, 0, ws>>>(P);
             else if (multi) k_electron<Real, true><<<ge, bs, 0, ws>>>(P);
             else k_electron<Real, false><<<ge, bs, 0, ws>>>(P);
@@ -2013,10 +2055,18 @@ struct Engine : EngineBase {
         const bool hfl = cfg.howfarless > 0;
         if (hfl && (Multi || mode)) { err = "HOWFARLESS transport is for one homogeneous phantom (no adjoint)"; return EGSGPU_ERR_ARG; }
         if (hfl && !homogeneous) { err = "HOWFARLESS transport needs a homogeneous phantom"; return EGSGPU_ERR_ARG; }
+        const bool pi = cfg.bca_algorithm == 1;
+        if (pi && (Multi || mode || hfl)) {
+            err = "PRESTA-I boundary crossing is for egsgpu_run (one phantom, no HOWFARLESS, no adjoint)";
+            return EGSGPU_ERR_ARG;
+        }
         if (hfl) {
             if (int rc = hfl_tables(err)) return rc;
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, false, false, true>, bs, 0));
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, false, false, true>, bs, 0));
+        } else if (pi) {
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, false>, bs, 0));
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, false, false, false, true>, bs, 0));
         } else if (adj) {
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, false, true>, bs, 0));
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, false, true>, bs, 0));
@@ -2458,6 +2508,8 @@ int egsgpu_load_media(egsgpu_handle *h, const char *data_dir, const char *pegs_f
     tp.ecut = h->cfg.ecut; tp.pcut = h->cfg.pcut;
     tp.estepe = h->cfg.estepe; tp.ximax = h->cfg.ximax; tp.skindepth_for_bca = h->cfg.skindepth;
     if (h->cfg.smax > 0) tp.smaxir = h->cfg.smax;
+    if (h->cfg.bca_algorithm != 0 && h->cfg.bca_algorithm != 1) { h->err = "bca_algorithm must be 0 (EXACT) or 1 (PRESTA-I)"; return EGSGPU_ERR_ARG; }
+    tp.exact_bca = h->cfg.bca_algorithm == 0;
     std::vector<std::string> nm;
     for (int i = 0; i < n; ++i) nm.push_back(names[i]);
     int rc = egs::hatch(data_dir, pegs_file, nm, tp, h->H, h->err);
@@ -2472,7 +2524,7 @@ int egsgpu_load_media(egsgpu_handle *h, const char *data_dir, const char *pegs_f
         return EGSGPU_ERR_ARG;
     }
     h->ecut = ecut; h->pcut = pcut;
-    rc = h->eng->load(h->H, ecut, pcut, h->cfg.skindepth, tp.smaxir, h->err);
+    rc = h->eng->load(h->H, ecut, pcut, h->H.params.skindepth_for_bca, tp.smaxir, h->err);
     if (rc) return rc;
     h->have_media = true;
     return 0;
@@ -2997,6 +3049,7 @@ int egsgpu_run_noalloc(egsgpu_handle *h, long long first, long long n, uint32_t 
         return EGSGPU_ERR_ARG;
     }
     if (!h->have_media || !h->have_geom || !h->have_source) { h->err = "media, geometry and source must be set"; return EGSGPU_ERR_STATE; }
+    if (h->cfg.bca_algorithm != 0) { h->err = "egsgpu_run_noalloc uses EXACT boundary crossing only"; return EGSGPU_ERR_ARG; }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) { h->err = "no current CUDA device"; return EGSGPU_ERR_CUDA; }
     unsigned char *scratch = nullptr;

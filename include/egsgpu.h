@@ -32,8 +32,8 @@ typedef struct egsgpu_handle egsgpu_handle;
 
 /* Transport parameters: the egs++ ":start MC transport parameter:" block
  * (egs++/egs_advanced_application.cpp:482-562) restricted to the physics
- * profile this engine implements (PRESTA-II, EXACT BCA, spin off, bound
- * Compton norej, Rayleigh on, EADL relaxation, Sauter photo-electrons,
+ * profile this engine implements (PRESTA-II, EXACT or PRESTA-I BCA, spin off,
+ * bound Compton norej, Rayleigh on, EADL relaxation, Sauter photo-electrons,
  * BH brems with KM angles, BH pair with simple angles). */
 typedef struct {
     double ecut;          /* global electron cut-off, total energy (MeV)   */
@@ -65,6 +65,13 @@ typedef struct {
                              (egs++/egs_advanced_application.cpp:487), the smaxir
                              limit on tmxs in ELECTR (src/egsnrc.mortran:1179);
                              <= 0 = no limit (1e10 cm, src/egsnrc.macros:2269) */
+    int bca_algorithm;    /* boundary crossing: 0 EXACT (default), 1 PRESTA-I: egs++
+                             "Boundary crossing algorithm" (bca_algorithm,
+                             src/egsnrc.mortran:2782-2783, 1247-1345).  With
+                             PRESTA-I a skindepth <= 1e-4 selects the old PRESTA
+                             default from the lowest ECUT (:2794-2815).  PRESTA-I
+                             is for egsgpu_run only (one phantom, no HOWFARLESS,
+                             no adjoint, not egsgpu_run_noalloc). */
 } egsgpu_config;
 
 /* Source: egs++ EGS_ParallelBeam (sources/egs_parallel_beam) with a point

@@ -151,6 +151,8 @@ struct Tally {
     std::vector<double> batch, sum, sum2;
     double dep = 0, esc = 0;
     double steps = 0, psteps = 0, esteps = 0, pushes = 0;
+    double tsteps = 0;   // charged-particle steps of non-zero length (AUSGAB(0) calls)
+    double msdist_calls = 0;   // PRESTA-II steps (count_pII_steps, egsnrc.mortran:4163)
     // optional record of every particle that leaves the phantom, ESC_REC
     // doubles each: charge, kinetic energy, x, y, z, u, v, w, weight, history
     bool log_esc = false;
@@ -1168,14 +1170,25 @@ newelectron:
             double p2 = eke * (eke + RMT2), beta2 = p2 / (p2 + RMSQ);
             double ssmfp = beta2 / blccl, skindepth = P.skindepth_for_bca * ssmfp;
             tustep = std::min(tustep, std::max(tperp, skindepth));
-            bool callhowfar, dosingle = false, callmsdist;
+            bool callhowfar, dosingle = false, callmsdist, domultiple = false;
             double ustep, uscat = 0, vscat = 0, wscat = 0, xtrans = 0, ytrans = 0, ztrans = 0;
+            // PRESTA-I multiple scattering of the step ($CALCULATE-XI, egsnrc.macros:1323-1348)
+            double ms_beta2 = 0, ms_chia2 = 0, ms_xi = 0;
+            const double xccl = rhof * m.xcc;
+            auto calculate_xi = [&](double ekems, double len) {
+                double pp2 = ekems * (ekems + RMT2);
+                ms_beta2 = pp2 / (pp2 + RMSQ);
+                ms_chia2 = xccl / (4 * blccl * pp2);
+                ms_xi = 0.5 * xccl / pp2 / ms_beta2 * len;
+                ms_xi = ms_xi * (std::log(1 + 1. / ms_chia2) - 1 / (1 + ms_chia2));
+            };
             R.T->steps += 1; R.T->esteps += 1;
-            if (tustep <= tperp && tustep > skindepth) {
+            if (tustep <= tperp && (!P.exact_bca || tustep > skindepth)) {
                 callhowfar = false; callmsdist = true;
+                R.T->msdist_calls += 1;
                 de = eloss_g(em, tustep, eke, elke, lelke, range, rhof);
                 msdist_pII(R, p, m, eke, de, tustep, rhof, qel, uscat, vscat, wscat, xtrans, ytrans, ztrans, ustep);
-            } else {
+            } else if (P.exact_bca) {
                 callmsdist = false;
                 double rnnoss = rnd(R, p);
                 if (rnnoss < 1.e-30) rnnoss = 1.e-30;
@@ -1192,7 +1205,17 @@ newelectron:
                 }
                 ustep = tustep;
                 callhowfar = !(ustep < tperp);
+            } else {
+                // boundary crossing a la EGS4/PRESTA-I with the exact path-length
+                // correction: $SET-USTEP (egsnrc.macros:1308-1321), egsnrc.mortran:1329-1345
+                callmsdist = false;
+                domultiple = true;
+                calculate_xi(eke - 0.5 * tustep * dedx, tustep);
+                ustep = ms_xi < 0.1 ? tustep * (1 - ms_xi * (0.5 - ms_xi * 0.166667))
+                                    : tustep * (1 - std::exp(-ms_xi)) / ms_xi;
+                callhowfar = !(ustep < tperp);
             }
+            const double ustep0 = ustep;
             int irold = p.ir, irnew = p.ir;
             if (callhowfar) irnew = O.hfl ? hfl_howfar(G, p, ustep) : howfar(G, p.ir, p, ustep);
             if (ustep <= 0) ustep = 0;
@@ -1209,10 +1232,19 @@ newelectron:
                 if (eie <= O.ecut) goto ecut_discard;
                 goto tstep_loop;
             }
+            R.T->tsteps += 1;
             double vstep = ustep, tvstep;
             if (callhowfar) {
-                tvstep = vstep;
-                if (tvstep != tustep) dosingle = false;
+                if (P.exact_bca) {
+                    tvstep = vstep;
+                    if (tvstep != tustep) dosingle = false;
+                } else if (vstep < ustep0) {
+                    // $SET-TVSTEP (egsnrc.macros:1350-1392)
+                    calculate_xi(eke - 0.5 * tustep * vstep / ustep0 * dedx, vstep);
+                    if (ms_xi < 0.1) tvstep = vstep * (1 + ms_xi * (0.5 + ms_xi * 0.333333));
+                    else if (ms_xi < 0.999999) tvstep = -vstep * std::log(1 - ms_xi) / ms_xi;
+                    else { ++R.errors; return; }
+                } else tvstep = tustep;
                 de = eloss_g(em, tvstep, eke, elke, lelke, range, rhof);
             } else {
                 tvstep = tustep;
@@ -1220,6 +1252,12 @@ newelectron:
             }
             double save_de = de, edep = de, ekef = eke - de;
             double costhe = 1, sinthe = 0;
+            if (!callmsdist && domultiple) {
+                // approximate CH step: one multiple-scattering deflection (egsnrc.mortran:1480-1496)
+                double lambda = blccl * tvstep / ms_beta2 / (1 + ms_chia2);
+                MsState st;
+                mscat(R, p, lambda, ms_chia2, ms_xi, st, costhe, sinthe);
+            }
             if (!callmsdist && dosingle) {
                 double ekems = std::max(ekef, O.ecut - RM);
                 double pp2 = ekems * (ekems + RMT2);
@@ -1233,7 +1271,7 @@ newelectron:
             if (callmsdist) { uf = uscat; vf = vscat; wf = wscat; xf = xtrans; yf = ytrans; zf = ztrans; }
             else {
                 xf = p.x + p.u * vstep; yf = p.y + p.v * vstep; zf = p.z + p.w * vstep;
-                if (dosingle) {
+                if (dosingle || domultiple) {
                     Azim az = azimuth(R, p);
                     rotate(p.u, p.v, p.w, sinthe, costhe, az, uf, vf, wf);
                 } else { uf = p.u; vf = p.v; wf = p.w; }
@@ -1588,11 +1626,15 @@ struct oracle_handle {
     long long hist_first = 0, hist_n = 0;
 };
 
-oracle_handle *oracle_create(const char *data_dir, const char *pegs, const char *const *names, int n,
-                             double ecut, double pcut) {
+// bca_algorithm: 0 EXACT, 1 PRESTA-I (egsnrc.mortran:2782-2783); skindepth
+// in elastic MFPs (PRESTA-I with skindepth <= 1e-4: the old PRESTA default).
+oracle_handle *oracle_create_bca(const char *data_dir, const char *pegs, const char *const *names, int n,
+                                 double ecut, double pcut, int bca_algorithm, double skindepth) {
     auto *h = new oracle_handle();
     TransportParams tp;
     tp.ecut = ecut; tp.pcut = pcut;
+    tp.exact_bca = bca_algorithm == 0;
+    tp.skindepth_for_bca = skindepth;
     std::vector<std::string> nm(names, names + n);
     std::string err;
     if (hatch(data_dir, pegs, nm, tp, h->O.H, err)) {
@@ -1606,6 +1648,19 @@ oracle_handle *oracle_create(const char *data_dir, const char *pegs, const char 
     h->O.pcut = pcut_eff;
     return h;
 }
+
+oracle_handle *oracle_create(const char *data_dir, const char *pegs, const char *const *names, int n,
+                             double ecut, double pcut) {
+    return oracle_create_bca(data_dir, pegs, names, n, ecut, pcut, 0, 3.0);
+}
+
+// The skin depth for boundary crossing in use (elastic MFPs).
+double oracle_skindepth(oracle_handle *h) { return h->O.H.params.skindepth_for_bca; }
+// Charged-particle steps of non-zero length so far (the AUSGAB(0) calls of
+// ELECTR; BEAMnrc's "total # charged particle steps").
+double oracle_charged_steps(oracle_handle *h) { return h->T.tsteps; }
+// PRESTA-II (msdist) steps so far.
+double oracle_msdist_steps(oracle_handle *h) { return h->T.msdist_calls; }
 
 void oracle_destroy(oracle_handle *h) { delete h; }
 
@@ -1686,6 +1741,7 @@ int oracle_run(oracle_handle *h, long long first, long long n, int nbatch, uint3
             h->T.esc_log.insert(h->T.esc_log.end(), t.esc_log.begin(), t.esc_log.end());
             h->T.dep += t.dep; h->T.esc += t.esc; h->T.steps += t.steps;
             h->T.psteps += t.psteps; h->T.esteps += t.esteps; h->T.pushes += t.pushes;
+            h->T.tsteps += t.tsteps; h->T.msdist_calls += t.msdist_calls;
         }
     }
     h->nhist += n;

@@ -25,6 +25,15 @@ def lib():
         vp, dp, i64 = C.c_void_p, C.POINTER(C.c_double), C.c_longlong
         L.oracle_create.restype = vp
         L.oracle_create.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(C.c_char_p), C.c_int, C.c_double, C.c_double]
+        L.oracle_create_bca.restype = vp
+        L.oracle_create_bca.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(C.c_char_p), C.c_int, C.c_double,
+                                        C.c_double, C.c_int, C.c_double]
+        L.oracle_skindepth.restype = C.c_double
+        L.oracle_skindepth.argtypes = [vp]
+        L.oracle_charged_steps.restype = C.c_double
+        L.oracle_charged_steps.argtypes = [vp]
+        L.oracle_msdist_steps.restype = C.c_double
+        L.oracle_msdist_steps.argtypes = [vp]
         L.oracle_destroy.argtypes = [vp]
         L.oracle_set_geometry.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp, dp, dp, C.POINTER(C.c_int32), dp]
         L.oracle_set_source.argtypes = [vp, C.c_void_p]
@@ -54,10 +63,13 @@ def _dp(a):
 
 
 class Oracle:
-    def __init__(self, media, ecut=0.521, pcut=0.010, pegs_file=PEGS_FILE):
+    def __init__(self, media, ecut=0.521, pcut=0.010, pegs_file=PEGS_FILE, bca_algorithm=0, skindepth=3.0):
+        """bca_algorithm 0: EXACT boundary crossing, 1: PRESTA-I (with
+        skindepth <= 1e-4 the old PRESTA default skin depth)."""
         L = lib()
         names = (C.c_char_p * len(media))(*[m.encode() for m in media])
-        h = L.oracle_create(DATA_DIR.encode(), pegs_file.encode(), names, len(media), ecut, pcut)
+        h = L.oracle_create_bca(DATA_DIR.encode(), pegs_file.encode(), names, len(media), ecut, pcut,
+                                int(bca_algorithm), float(skindepth))
         if not h:
             raise RuntimeError("oracle: media load failed")
         self.h = C.c_void_p(h)
@@ -74,6 +86,18 @@ class Oracle:
     def set_howfarless(self, on=True):
         """DOSXYZnrc HOWFARLESS transport in the current (homogeneous) phantom."""
         assert self.L.oracle_set_howfarless(self.h, int(bool(on))) == 0
+
+    def skindepth(self):
+        """The skin depth for boundary crossing in use (elastic MFPs)."""
+        return self.L.oracle_skindepth(self.h)
+
+    def charged_steps(self):
+        """Charged-particle steps of non-zero length so far."""
+        return self.L.oracle_charged_steps(self.h)
+
+    def msdist_steps(self):
+        """PRESTA-II (msdist) steps so far."""
+        return self.L.oracle_msdist_steps(self.h)
 
     def set_smax(self, smax):
         """Maximum charged-particle step in cm (<= 0: no limit)."""

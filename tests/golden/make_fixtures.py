@@ -10,7 +10,8 @@
                                EXslabs.egslst and EXphantom.egslst (BEAMnrc,
                                EGSnrc, 2004) print for those runs: dose per
                                zone with its uncertainty, the scoring-plane
-                               fluence and the phase-space source counts that
+                               fluence, the step counts, the PRESTA-I skin
+                               depth and the phase-space source counts that
                                set the dose normalisation
 
 Usage: python tests/golden/make_fixtures.py <HEN_HOUSE>
@@ -86,6 +87,9 @@ def listings(hh):
         "EXslabs": dict(
             dose=dose_zones(slabs),
             charged_steps_per_history=value_pct(slabs, "# CHARGED PARTICLE STEPS/INITIAL HISTORY"),
+            presta2_step_fraction=value_pct(slabs, "# PRESTA-II STEPS/TOTAL # CHARGED PARTICLE STEPS"),
+            skindepth_mfp=int_after(slabs, "Skin-depth for boundary crossing (MFP)"),
+            brems_events=int_after(slabs, "NO. OF BREMSSTRAHLUNG EVENTS IN THIS RUN:"),
             histories=int_after(slabs, "Max # of histories: to run"),
             plane_radii_cm=[_f(x) for x in radii.split()[4:]],
             plane_electrons=plane_zone1(slabs, "ELECTRONS"),

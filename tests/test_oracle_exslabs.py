@@ -10,12 +10,13 @@ back face; its phase-space file (EXslabs.egsphsp1) holds those particles.
 Both are fixtures here (tests/golden/beamnrc_examples.json, generated from the
 listing by tests/golden/make_fixtures.py, and EXslabs.egsphsp1.gz).
 
-The reference ran with spin effects on and the PRESTA-I boundary-crossing
-algorithm; this restatement has neither, and neither matters here at the
-listing's precision: the energy deposit in a thin, homogeneous slab is set by
-stopping powers, Moller/bremsstrahlung production and escape.  (The number of
-charged-particle steps does depend on the boundary-crossing algorithm and is
-not compared.)
+The reference ran with spin effects on (not restated: the spin data file is
+not part of the reference) and the PRESTA-I boundary-crossing algorithm.  The
+listing's deposit and fluences are compared for both boundary-crossing
+algorithms of the restatement, EXACT and PRESTA-I: in a thin, homogeneous slab
+they are set by stopping powers, Moller/bremsstrahlung production and escape.
+The step counts depend on the boundary-crossing algorithm and are compared for
+PRESTA-I only, with the skin depth that PRESTA-I derives from ECUT.
 """
 import json
 import os
@@ -53,10 +54,16 @@ def deposit_reference():
     return e, e * z["sigma_pct"] / 100
 
 
-@pytest.fixture(scope="module")
-def oracle_run():
+def exslabs_oracle(bca_algorithm):
+    """The oracle set up as EXslabs ran: PRESTA-I takes the default skin depth."""
+    return Oracle(["AIR700ICRU"], ecut=1.0, pcut=0.01, pegs_file=PEGS700, bca_algorithm=bca_algorithm,
+                  skindepth=0.0 if bca_algorithm else 3.0)
+
+
+@pytest.fixture(scope="module", params=[0, 1], ids=["exact", "presta1"])
+def oracle_run(request):
     g, src = exslabs_case()
-    o = Oracle(["AIR700ICRU"], ecut=1.0, pcut=0.01, pegs_file=PEGS700)
+    o = exslabs_oracle(request.param)
     o.set_geometry(g)
     o.set_source(src)
     o.set_smax(5.0)
@@ -65,8 +72,11 @@ def oracle_run():
     o.run(n, nbatch=nb, seed=2004, threads=8)
     s, s2, tot = o.tallies()
     esc = o.escapes()
+    run = (n, nb, s, s2, tot, esc)
+    if request.param == 1:
+        run += (o.charged_steps(), o.msdist_steps())
     o.close()
-    return n, nb, s, s2, tot, esc
+    return run
 
 
 def test_listing_fixture():
@@ -78,7 +88,7 @@ def test_listing_fixture():
 
 
 def test_energy_deposit_matches_reference_run(oracle_run):
-    n, nb, s, s2, tot, _ = oracle_run
+    n, nb, s, s2, tot, _ = oracle_run[:6]
     m = s[0] / nb
     sig = np.sqrt(max(s2[0] / nb - m * m, 0) / (nb - 1)) * nb / n
     dep = s[0] / n
@@ -93,7 +103,7 @@ def _back(esc):
 
 
 def test_back_plane_fluence_matches_listing(oracle_run):
-    n, _, _, _, _, esc = oracle_run
+    n, _, _, _, _, esc = oracle_run[:6]
     L = listing()
     r1 = L["plane_radii_cm"][0]
     b = _back(esc)
@@ -124,7 +134,7 @@ def test_exit_electrons_match_reference_phase_space(oracle_run):
     than 0.3 MeV (a Moller or bremsstrahlung event) within 3 sigma, and
     two-sample Kolmogorov-Smirnov tests of the radius and polar angle."""
     stats = pytest.importorskip("scipy.stats")
-    n, _, _, _, _, esc = oracle_run
+    n, _, _, _, _, esc = oracle_run[:6]
     ref, hdr = F.read_egsphsp(os.path.join(GOLD, "EXslabs.egsphsp1.gz"))
     assert hdr["incident"] == 1000
     re_ = ref[ref[:, 0] == -1]
@@ -140,3 +150,24 @@ def test_exit_electrons_match_reference_phase_space(oracle_run):
     ]
     for mine, theirs in pairs:
         assert stats.ks_2samp(mine, theirs).pvalue > 1e-3
+
+
+def test_presta1_default_skindepth_is_the_listings():
+    """PRESTA-I with no skin depth given: the old PRESTA minimum step from the
+    lowest ECUT, which the listing prints (910.8 elastic MFPs)."""
+    assert exslabs_oracle(1).skindepth() == pytest.approx(listing()["skindepth_mfp"], abs=0.05)
+    assert exslabs_oracle(0).skindepth() == 3.0
+
+
+def test_presta1_step_counts_match_listing(oracle_run):
+    """Charged-particle steps per history (21.22 +- 0.3%) and their PRESTA-II
+    fraction (0.859 +- 0.3%) as the reference counted them (AUSGAB(0) calls,
+    msdist_pII calls).  The restatement gives 0.8-0.9% fewer of both, which
+    this test allows: the listing comes from the EGSnrc of 2004 with spin
+    effects on."""
+    if len(oracle_run) < 8:
+        pytest.skip("step counts are compared for PRESTA-I")
+    n, steps, msdist = oracle_run[0], oracle_run[6], oracle_run[7]
+    L = listing()
+    assert steps / n == pytest.approx(L["charged_steps_per_history"]["value"], rel=0.015)
+    assert msdist / steps == pytest.approx(L["presta2_step_fraction"]["value"], rel=0.015)

@@ -128,9 +128,11 @@ def run_app(tmp_path, text, name):
 
 
 def compare(dose_file, dose_py):
+    # the file holds %g of the single-precision dose (6 digits); doses are
+    # ~1e-11 Gy per history, so the comparison is relative only
     sel = dose_py > 1e-3 * dose_py.max()
     assert sel.sum() > 5
-    assert np.allclose(dose_file[sel], dose_py[sel].astype(np.float32), rtol=2e-5)
+    assert np.allclose(dose_file[sel], dose_py[sel].astype(np.float32), rtol=2e-5, atol=0)
 
 
 def test_app_slab_matches_binding(tmp_path):
@@ -159,3 +161,24 @@ def test_app_phase_space_source_matches_binding(tmp_path):
     eng.set_source(eg.PhaseSpaceSource(p, position=(0, 0, -0.5), recycle=1))
     eng.run(30000, nbatch=3, seed=3)
     compare(dose_file, eng.dose()[0])
+
+
+def test_app_presta1_and_smax_match_binding(tmp_path):
+    """The transport keys "Boundary crossing algorithm = PRESTA-I", "Skin
+    depth for BCA" and "Global Smax" reach the engine as the binding sets them."""
+    text = SLAB.replace("    Global PCUT = 0.01\n", "    Global PCUT = 0.01\n    Boundary crossing algorithm = PRESTA-I\n"
+                        "    Skin depth for BCA = 0\n    Global Smax = 0.3\n")
+    dose_file, _ = run_app(tmp_path, text, "slab_p1")
+    zb = 0.5 * np.arange(21)
+    med = np.zeros(len(zb) - 1, dtype=np.int32)
+    med[4:7] = 1
+    g = eg.XYZGeometry([-5, 5], [-5, 5], zb, med)
+    eng = eg.DoseEngine([W.WATER, W.BONE], ecut=0.7, pcut=0.01, bca_algorithm=1, skindepth=0.0, smax=0.3)
+    eng.set_geometry(g)
+    eng.set_source(eg.ParallelBeam(charge=-1, energy=12.0, position=(0, 0, -8)))
+    eng.run(40000, nbatch=4, seed=7)
+    compare(dose_file, eng.dose()[0])
+    # and they changed the transport: the EXACT run of the same input differs
+    exact, _ = run_app(tmp_path, SLAB, "slab_exact")
+    sel = dose_file > 1e-3 * dose_file.max()
+    assert np.max(np.abs(exact[sel] / dose_file[sel] - 1)) > 1e-3

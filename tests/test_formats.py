@@ -47,7 +47,8 @@ def test_3ddose_roundtrip(tmp_path):
     formats.write_3ddose(p, g, d, s)
     (nx, ny, nz), (xb, yb, zb), d2, r2 = formats.read_3ddose(p)
     assert (nx, ny, nz) == (6, 6, 6)
-    assert np.allclose(d2, d.astype(np.float32), rtol=1e-6)
+    # %g keeps 6 significant digits (<= 5e-6 relative); doses ~1e-12 need atol=0
+    assert np.allclose(d2, d.astype(np.float32), rtol=5e-6, atol=0)
     assert r2[3] == 1.0 and np.allclose(r2[d > 0], 0.01, rtol=1e-5)
 
 

@@ -36,19 +36,22 @@ def _newer(target, sources):
 
 
 def build_engine(force=False):
-    srcs = [os.path.join(CSRC, f) for f in ("egs_transport.cu", "egs_hatch.cpp")]
+    srcs = [os.path.join(CSRC, f) for f in ("egs_transport.cu", "egs_hatch.cpp", "egs_transport_f64.cu")]
     deps = srcs + [os.path.join(CSRC, f) for f in ("egs_device.cuh", "egs_physics.cuh", "egs_hatch.h")] + [
         os.path.join(ROOT, "include", "egsgpu.h")]
     if not force and _newer(LIB, deps):
         return LIB
     bdir = os.path.join(HERE, "_build")
     os.makedirs(bdir, exist_ok=True)
-    objs = [os.path.join(bdir, "egs_transport.o"), os.path.join(bdir, "egs_hatch.o")]
+    objs = [os.path.join(bdir, "egs_transport.o"), os.path.join(bdir, "egs_hatch.o"),
+            os.path.join(bdir, "egs_transport_f64.o")]
     cmds = [
         [NVCC] + ARCH + NVFLAGS + ["-c", srcs[0], "-o", objs[0]],
         ["g++", "-O2", "-std=c++17", "-fPIC", "-c", srcs[1], "-o", objs[1]],
+        # the FP64 engine rounds like the CPU oracle: no fused multiply-adds
+        [NVCC] + ARCH + NVFLAGS + ["--fmad=false", "-c", srcs[2], "-o", objs[2]],
     ]
-    with ThreadPoolExecutor(2) as ex:
+    with ThreadPoolExecutor(3) as ex:
         list(ex.map(_run, cmds))
     _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
     return LIB

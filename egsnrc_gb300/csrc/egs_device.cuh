@@ -137,7 +137,8 @@ __host__ __device__ inline uint64_t child_sid(uint64_t sid, uint32_t n, uint32_t
 // One Philox block, kept out of line: the generator is called from about a
 // hundred places in the transport kernels and inlining its ten rounds at each
 // would multiply the kernels' instruction footprint.
-__device__ __noinline__ uint4 philox_block(uint32_t b, uint32_t s0, uint32_t s1, uint32_t k0, uint32_t k1);
+// (internal linkage: each translation unit of the engine has its own copy)
+static __device__ __noinline__ uint4 philox_block(uint32_t b, uint32_t s0, uint32_t s1, uint32_t k0, uint32_t k1);
 
 struct Rng {
     uint32_t seed, hist, n, blk;

@@ -40,13 +40,23 @@
 
 namespace cg = cooperative_groups;
 
+// This file is compiled twice: as itself (the FP32 engine and the C ABI) and,
+// through egs_transport_f64.cu, as the FP64 engine without fused multiply-adds.
+// Each compilation keeps its kernels, device constants and engine in its own
+// namespace, EGSGPU_TU, so that the two share no symbol.
+#ifndef EGSGPU_TU
+#define EGSGPU_TU tu32
+#endif
+
 namespace egsgpu {
 
-__device__ __noinline__ uint4 philox_block(uint32_t b, uint32_t s0, uint32_t s1, uint32_t k0, uint32_t k1) {
+static __device__ __noinline__ uint4 philox_block(uint32_t b, uint32_t s0, uint32_t s1, uint32_t k0, uint32_t k1) {
     uint32_t o[4];
     philox10(b, s0, s1, 0u, k0, k1, o);
     return make_uint4(o[0], o[1], o[2], o[3]);
 }
+
+namespace EGSGPU_TU {
 
 __constant__ MedScalars<float> c_med_f[MAXMED];
 __constant__ MedScalars<double> c_med_d[MAXMED];
@@ -1525,14 +1535,16 @@ __global__ void k_batch(double *d, double *sum, double *sum2, long long n) {
     }
 }
 
+}  // namespace EGSGPU_TU
 }  // namespace egsgpu
 
 // ===================================================================
 //                         host-side engine
 // ===================================================================
 using namespace egsgpu;
+using namespace egsgpu::EGSGPU_TU;
 
-namespace {
+namespace egsgpu_host {
 
 #define CK(x)                                                                                 \
     do {                                                                                      \
@@ -1542,6 +1554,48 @@ namespace {
             return EGSGPU_ERR_CUDA;                                                           \
         }                                                                                     \
     } while (0)
+
+// One phantom of a multi-phantom run, as handed to the engine.
+struct PhantomDesc {
+    int nx, ny, nz;
+    const double *xb, *yb, *zb;
+    const int32_t *med;
+    const double *rhor;
+    uint32_t seed;
+    long long histories;
+};
+
+// The engine behind a handle: one implementation per precision (Engine<float>
+// here, Engine<double> in the FP64 translation unit).
+struct EngineBase {
+    virtual ~EngineBase() {}
+    virtual int load(const egs::Hatch &H, double ecut, double pcut, double skindepth, double smax,
+                     std::string &err) = 0;
+    virtual int geometry(int nx, int ny, int nz, const double *xb, const double *yb, const double *zb,
+                         const int32_t *med, const double *rhor, std::string &err) = 0;
+    virtual int run(const Source &S, long long first, long long n, int nbatch, uint32_t seed, cudaStream_t st,
+                    std::string &err) = 0;
+    virtual int run_noalloc(const Source &S, long long first, long long n, uint32_t seed, double *dose,
+                            cudaStream_t st, unsigned char *scratch, size_t scratch_bytes, std::string &err) = 0;
+    virtual int problems(int n, const PhantomDesc *pd, const Source *src, std::string &err) = 0;
+    virtual int run_multi(const Source &Smax, int nbatch, cudaStream_t st, std::string &err) = 0;
+    virtual int adjoint(const Source &S, long long first, long long n, uint32_t seed, const double *w, double *grad,
+                        std::string &err) = 0;
+    // tallies and counters of the runs so far
+    virtual int clear_tallies(long long nv, std::string &err) = 0;
+    virtual int read_sums(long long off, long long n, double *sum, double *sum2, std::string &err) = 0;
+    virtual int read_totals(double *energy2, unsigned long long *counters, std::string &err) = 0;   // CNT_N counters
+    virtual int restore_sums(const double *energy2, const unsigned long long *counters8, const double *sum,
+                             const double *sum2, long long nv, std::string &err) = 0;
+    virtual int read_profile(double *out18, std::string &err) = 0;
+    virtual int history_tally(long long first, long long n, std::string &err) = 0;
+    virtual int read_history_tally(double *out, std::string &err) = 0;
+};
+
+// The FP64 engine, built in its own translation unit (egs_transport_f64.cu).
+EngineBase *make_engine_f64(const egsgpu_config &c);
+
+namespace EGSGPU_TU {
 
 // Multiplier and shift for dividing by d with a multiply-high, an add and a
 // shift: l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1; then
@@ -1642,35 +1696,66 @@ struct DevMem {
     }
 };
 
-// One phantom of a multi-phantom run, as handed to the engine.
-struct PhantomDesc {
-    int nx, ny, nz;
-    const double *xb, *yb, *zb;
-    const int32_t *med;
-    const double *rhor;
-    uint32_t seed;
-    long long histories;
-};
-
-struct EngineBase {
-    virtual ~EngineBase() {}
-    virtual int load(const egs::Hatch &H, double ecut, double pcut, double skindepth, double smax,
-                     std::string &err) = 0;
-    virtual int geometry(int nx, int ny, int nz, const double *xb, const double *yb, const double *zb,
-                         const int32_t *med, const double *rhor, std::string &err) = 0;
-    virtual int run(const Source &S, long long first, long long n, int nbatch, uint32_t seed, cudaStream_t st,
-                    std::string &err) = 0;
-    virtual int run_noalloc(const Source &S, long long first, long long n, uint32_t seed, double *dose,
-                            cudaStream_t st, unsigned char *scratch, size_t scratch_bytes, std::string &err) = 0;
-    virtual int problems(int n, const PhantomDesc *pd, const Source *src, std::string &err) = 0;
-    virtual int run_multi(const Source &Smax, int nbatch, cudaStream_t st, std::string &err) = 0;
-    virtual int adjoint(const Source &S, long long first, long long n, uint32_t seed, const double *w, double *grad,
-                        std::string &err) = 0;
-};
-
 template <class Real>
 struct Engine : EngineBase {
     egsgpu_config cfg;
+
+    int clear_tallies(long long nv, std::string &err) override {
+        CK(cudaMemset(d_dose.p, 0, nv * sizeof(double)));
+        CK(cudaMemset(d_sum.p, 0, nv * sizeof(double)));
+        CK(cudaMemset(d_sum2.p, 0, nv * sizeof(double)));
+        CK(cudaMemset(d_energy.p, 0, 2 * sizeof(double)));
+        CK(cudaMemset(d_counters.p, 0, CNT_N * sizeof(unsigned long long)));
+        CK(cudaMemset(d_error.p, 0, 2 * sizeof(int)));
+        for (int k = 0; k < 4; ++k) { prof_ms[k] = 0; prof_n[k] = 0; }
+        return 0;
+    }
+    int read_sums(long long off, long long n, double *sum, double *sum2, std::string &err) override {
+        if (sum) CK(cudaMemcpy(sum, (double *)d_sum.p + off, n * sizeof(double), cudaMemcpyDeviceToHost));
+        if (sum2) CK(cudaMemcpy(sum2, (double *)d_sum2.p + off, n * sizeof(double), cudaMemcpyDeviceToHost));
+        return 0;
+    }
+    int read_totals(double *energy2, unsigned long long *counters, std::string &err) override {
+        if (energy2) CK(cudaMemcpy(energy2, d_energy.p, 2 * sizeof(double), cudaMemcpyDeviceToHost));
+        if (counters) CK(cudaMemcpy(counters, d_counters.p, CNT_N * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+        return 0;
+    }
+    int restore_sums(const double *energy2, const unsigned long long *counters8, const double *sum,
+                     const double *sum2, long long nv, std::string &err) override {
+        CK(cudaMemcpy(d_energy.p, energy2, 2 * sizeof(double), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d_counters.p, counters8, 8 * sizeof(unsigned long long), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d_sum.p, sum, nv * sizeof(double), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d_sum2.p, sum2, nv * sizeof(double), cudaMemcpyHostToDevice));
+        CK(cudaMemset(d_dose.p, 0, nv * sizeof(double)));
+        return 0;
+    }
+    int read_profile(double *out, std::string &err) override {
+        unsigned long long c[CNT_N];
+        CK(cudaMemcpy(c, d_counters.p, sizeof(c), cudaMemcpyDeviceToHost));
+        for (int k = 0; k < 4; ++k) { out[k] = prof_ms[k]; out[4 + k] = (double)prof_n[k]; }
+        out[8] = (double)c[CNT_PSTEP]; out[9] = (double)c[CNT_ESTEP];
+        out[10] = (double)c[CNT_PUSH]; out[11] = (double)c[CNT_EPUSH];
+        out[12] = (double)c[CNT_INTER]; out[13] = (double)c[CNT_EINTER];
+        out[14] = (double)tuned_chunk;
+        out[15] = gexec ? 1.0 : 0.0;
+        out[16] = c[CNT_PITER] ? (double)c[CNT_PLANES] / c[CNT_PITER] : 0.0;
+        out[17] = c[CNT_EITER] ? (double)c[CNT_ELANES] / c[CNT_EITER] : 0.0;
+        return 0;
+    }
+    int history_tally(long long first, long long n, std::string &err) override {
+        hist_first = first;
+        hist_n = n;
+        if (n > 0) {
+            CK(d_hist.alloc(n * sizeof(double)));
+            CK(cudaMemset(d_hist.p, 0, n * sizeof(double)));
+        }
+        return 0;
+    }
+    int read_history_tally(double *out, std::string &err) override {
+        if (hist_n > 0) CK(cudaMemcpy(out, d_hist.p, hist_n * sizeof(double), cudaMemcpyDeviceToHost));
+        return 0;
+    }
+
     int nmed = 0;
     std::vector<MedScalars<Real>> meds;
     DevMem d_etab, d_erange, d_gtab, d_pmax, d_ray, d_rayi, d_shell, d_shellat, d_elem, d_ms, d_msi;
@@ -2424,7 +2509,16 @@ struct Engine : EngineBase {
     }
 };
 
-}  // namespace
+}  // namespace EGSGPU_TU
+}  // namespace egsgpu_host
+
+using namespace egsgpu_host;
+using namespace egsgpu_host::EGSGPU_TU;
+
+#ifdef EGSGPU_PART_F64
+// The FP64 translation unit contributes its engine only.
+EngineBase *egsgpu_host::make_engine_f64(const egsgpu_config &c) { return new Engine<double>(c); }
+#else
 
 struct egsgpu_handle {
     egsgpu_config cfg;
@@ -2460,17 +2554,13 @@ struct egsgpu_handle {
     long long nvox() const { return multi() ? mvox : (long long)nx * ny * nz; }
 };
 
-template <class E>
-static int get_tallies_impl(egsgpu_handle *h, E *eng, double *sum, double *sum2, double *totals) {
-    std::string &err = h->err;
+static int get_tallies_impl(egsgpu_handle *h, double *sum, double *sum2, double *totals) {
     long long nv = h->nvox();
-    if (sum) CK(cudaMemcpy(sum, eng->d_sum.p, nv * sizeof(double), cudaMemcpyDeviceToHost));
-    if (sum2) CK(cudaMemcpy(sum2, eng->d_sum2.p, nv * sizeof(double), cudaMemcpyDeviceToHost));
+    if (int rc = h->eng->read_sums(0, nv, sum, sum2, h->err)) return rc;
     if (totals) {
         double en[2];
         unsigned long long c[CNT_N];
-        CK(cudaMemcpy(en, eng->d_energy.p, sizeof(en), cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(c, eng->d_counters.p, sizeof(c), cudaMemcpyDeviceToHost));
+        if (int rc = h->eng->read_totals(en, c, h->err)) return rc;
         totals[0] = (double)h->nhist; totals[1] = h->nbatch; totals[2] = en[0]; totals[3] = en[1];
         totals[4] = (double)(c[CNT_PSTEP] + c[CNT_ESTEP]); totals[5] = (double)c[CNT_PSTEP];
         totals[6] = (double)c[CNT_ESTEP]; totals[7] = (double)(c[CNT_PUSH] + c[CNT_EPUSH]);
@@ -2496,7 +2586,7 @@ int egsgpu_create(const egsgpu_config *cfg, egsgpu_handle **out) {
     auto *h = new egsgpu_handle();
     h->cfg = *cfg;
     if (cfg->precision == 32) h->eng.reset(new Engine<float>(*cfg));
-    else h->eng.reset(new Engine<double>(*cfg));
+    else h->eng.reset(make_engine_f64(*cfg));
     *out = h;
     return 0;
 }
@@ -2817,14 +2907,6 @@ int egsgpu_get_phantom_info(egsgpu_handle *h, int k, long long *out) {
 
 }  // extern "C"
 
-template <class E>
-static int read_range_impl(egsgpu_handle *h, E *eng, long long off, long long n, double *sum, double *sum2) {
-    std::string &err = h->err;
-    if (sum) CK(cudaMemcpy(sum, (double *)eng->d_sum.p + off, n * sizeof(double), cudaMemcpyDeviceToHost));
-    if (sum2) CK(cudaMemcpy(sum2, (double *)eng->d_sum2.p + off, n * sizeof(double), cudaMemcpyDeviceToHost));
-    return 0;
-}
-
 extern "C" {
 
 int egsgpu_get_phantom_dose(egsgpu_handle *h, int k, double *dose, double *sigma) {
@@ -2832,8 +2914,7 @@ int egsgpu_get_phantom_dose(egsgpu_handle *h, int k, double *dose, double *sigma
     const auto &P = h->phantoms[k];
     long long nv = (long long)P.nx * P.ny * P.nz;
     std::vector<double> s(nv), s2(nv);
-    int rc = h->cfg.precision == 32 ? read_range_impl(h, (Engine<float> *)h->eng.get(), P.voff, nv, s.data(), s2.data())
-                                    : read_range_impl(h, (Engine<double> *)h->eng.get(), P.voff, nv, s.data(), s2.data());
+    int rc = h->eng->read_sums(P.voff, nv, s.data(), s2.data(), h->err);
     if (rc) return rc;
     const double N = (double)P.nhist, nb = (double)h->nbatch;
     for (long long i = 0; i < nv; ++i) {
@@ -2853,21 +2934,7 @@ int egsgpu_get_phantom_dose(egsgpu_handle *h, int k, double *dose, double *sigma
 
 int egsgpu_reset(egsgpu_handle *h) {
     if (!h || !h->have_geom) return EGSGPU_ERR_STATE;
-    std::string &err = h->err;
-    EngineBase *e = h->eng.get();
-    (void)e;
-    long long nv = h->nvox();
-    auto reset = [&](auto *eng) -> int {
-        CK(cudaMemset(eng->d_dose.p, 0, nv * sizeof(double)));
-        CK(cudaMemset(eng->d_sum.p, 0, nv * sizeof(double)));
-        CK(cudaMemset(eng->d_sum2.p, 0, nv * sizeof(double)));
-        CK(cudaMemset(eng->d_energy.p, 0, 2 * sizeof(double)));
-        CK(cudaMemset(eng->d_counters.p, 0, CNT_N * sizeof(unsigned long long)));
-        CK(cudaMemset(eng->d_error.p, 0, 2 * sizeof(int)));
-        for (int k = 0; k < 4; ++k) { eng->prof_ms[k] = 0; eng->prof_n[k] = 0; }
-        return 0;
-    };
-    int rc = h->cfg.precision == 32 ? reset((Engine<float> *)h->eng.get()) : reset((Engine<double> *)h->eng.get());
+    int rc = h->eng->clear_tallies(h->nvox(), h->err);
     if (rc) return rc;
     h->nhist = 0; h->nbatch = 0;
     for (auto &P : h->phantoms) P.nhist = 0;
@@ -2877,27 +2944,12 @@ int egsgpu_reset(egsgpu_handle *h) {
 int egsgpu_get_profile(egsgpu_handle *h, double *out) {
     // out[18]; see include/egsgpu.h
     if (!h || !out || !h->have_geom) return EGSGPU_ERR_ARG;
-    std::string &err = h->err;
-    auto get = [&](auto *eng) -> int {
-        unsigned long long c[CNT_N];
-        CK(cudaMemcpy(c, eng->d_counters.p, sizeof(c), cudaMemcpyDeviceToHost));
-        for (int k = 0; k < 4; ++k) { out[k] = eng->prof_ms[k]; out[4 + k] = (double)eng->prof_n[k]; }
-        out[8] = (double)c[CNT_PSTEP]; out[9] = (double)c[CNT_ESTEP];
-        out[10] = (double)c[CNT_PUSH]; out[11] = (double)c[CNT_EPUSH];
-        out[12] = (double)c[CNT_INTER]; out[13] = (double)c[CNT_EINTER];
-        out[14] = (double)eng->tuned_chunk;
-        out[15] = eng->gexec ? 1.0 : 0.0;
-        out[16] = c[CNT_PITER] ? (double)c[CNT_PLANES] / c[CNT_PITER] : 0.0;
-        out[17] = c[CNT_EITER] ? (double)c[CNT_ELANES] / c[CNT_EITER] : 0.0;
-        return 0;
-    };
-    return h->cfg.precision == 32 ? get((Engine<float> *)h->eng.get()) : get((Engine<double> *)h->eng.get());
+    return h->eng->read_profile(out, h->err);
 }
 
 int egsgpu_get_tallies(egsgpu_handle *h, double *sum, double *sum2, double *totals) {
     if (!h || !h->have_geom) return EGSGPU_ERR_STATE;
-    if (h->cfg.precision == 32) return get_tallies_impl(h, (Engine<float> *)h->eng.get(), sum, sum2, totals);
-    return get_tallies_impl(h, (Engine<double> *)h->eng.get(), sum, sum2, totals);
+    return get_tallies_impl(h, sum, sum2, totals);
 }
 
 int egsgpu_get_dose(egsgpu_handle *h, double *dose, double *sigma) {
@@ -2953,27 +3005,12 @@ int egsgpu_adjoint(egsgpu_handle *h, long long first, long long n, uint32_t seed
 
 int egsgpu_set_history_tally(egsgpu_handle *h, long long first, long long n) {
     if (!h || n < 0 || n > (1LL << 24)) return EGSGPU_ERR_ARG;
-    std::string &err = h->err;
-    auto set = [&](auto *eng) -> int {
-        eng->hist_first = first;
-        eng->hist_n = n;
-        if (n > 0) {
-            CK(eng->d_hist.alloc(n * sizeof(double)));
-            CK(cudaMemset(eng->d_hist.p, 0, n * sizeof(double)));
-        }
-        return 0;
-    };
-    return h->cfg.precision == 32 ? set((Engine<float> *)h->eng.get()) : set((Engine<double> *)h->eng.get());
+    return h->eng->history_tally(first, n, h->err);
 }
 
 int egsgpu_get_history_tally(egsgpu_handle *h, double *out) {
     if (!h || !out) return EGSGPU_ERR_ARG;
-    std::string &err = h->err;
-    auto get = [&](auto *eng) -> int {
-        if (eng->hist_n > 0) CK(cudaMemcpy(out, eng->d_hist.p, eng->hist_n * sizeof(double), cudaMemcpyDeviceToHost));
-        return 0;
-    };
-    return h->cfg.precision == 32 ? get((Engine<float> *)h->eng.get()) : get((Engine<double> *)h->eng.get());
+    return h->eng->read_history_tally(out, h->err);
 }
 
 // Checkpoint layout: magic, nvox, nhist, nbatch, energy[2], counters[8], sum[nvox], sum2[nvox]
@@ -2983,19 +3020,20 @@ int egsgpu_checkpoint(egsgpu_handle *h, void *buf, size_t *size) {
     size_t need = 8 * 4 + 2 * 8 + 8 * 8 + 2 * nv * 8;
     if (!buf) { *size = need; return 0; }
     if (*size < need) { *size = need; h->err = "checkpoint buffer too small"; return EGSGPU_ERR_ARG; }
-    std::string &err = h->err;
     char *b = (char *)buf;
     long long hdr[4] = {0x45475347505531LL, nv, h->nhist, h->nbatch};
     std::memcpy(b, hdr, 32);
-    auto dump = [&](auto *eng) -> int {
-        CK(cudaMemcpy(b + 32, eng->d_energy.p, 16, cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(b + 48, eng->d_counters.p, 64, cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(b + 112, eng->d_sum.p, nv * 8, cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(b + 112 + nv * 8, eng->d_sum2.p, nv * 8, cudaMemcpyDeviceToHost));
-        return 0;
-    };
+    double en[2];
+    unsigned long long c[CNT_N];
+    if (int rc = h->eng->read_totals(en, c, h->err)) return rc;
+    std::memcpy(b + 32, en, 16);
+    std::memcpy(b + 48, c, 64);   // the first 8 counters
+    std::vector<double> s(nv), s2(nv);
+    if (int rc = h->eng->read_sums(0, nv, s.data(), s2.data(), h->err)) return rc;
+    std::memcpy(b + 112, s.data(), nv * 8);
+    std::memcpy(b + 112 + nv * 8, s2.data(), nv * 8);
     *size = need;
-    return h->cfg.precision == 32 ? dump((Engine<float> *)h->eng.get()) : dump((Engine<double> *)h->eng.get());
+    return 0;
 }
 
 int egsgpu_restore(egsgpu_handle *h, const void *buf, size_t size) {
@@ -3007,16 +3045,14 @@ int egsgpu_restore(egsgpu_handle *h, const void *buf, size_t size) {
     if (size < need) { h->err = "checkpoint too small"; return EGSGPU_ERR_ARG; }
     std::memcpy(hdr, b, 32);
     if (hdr[0] != 0x45475347505531LL || hdr[1] != nv) { h->err = "checkpoint does not match this geometry"; return EGSGPU_ERR_ARG; }
-    std::string &err = h->err;
-    auto load = [&](auto *eng) -> int {
-        CK(cudaMemcpy(eng->d_energy.p, b + 32, 16, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(eng->d_counters.p, b + 48, 64, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(eng->d_sum.p, b + 112, nv * 8, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(eng->d_sum2.p, b + 112 + nv * 8, nv * 8, cudaMemcpyHostToDevice));
-        CK(cudaMemset(eng->d_dose.p, 0, nv * 8));
-        return 0;
-    };
-    int rc = h->cfg.precision == 32 ? load((Engine<float> *)h->eng.get()) : load((Engine<double> *)h->eng.get());
+    double en[2];
+    unsigned long long c[8];
+    std::vector<double> s(nv), s2(nv);
+    std::memcpy(en, b + 32, 16);
+    std::memcpy(c, b + 48, 64);
+    std::memcpy(s.data(), b + 112, nv * 8);
+    std::memcpy(s2.data(), b + 112 + nv * 8, nv * 8);
+    int rc = h->eng->restore_sums(en, c, s.data(), s2.data(), nv, h->err);
     if (rc) return rc;
     h->nhist = hdr[2];
     h->nbatch = (int)hdr[3];
@@ -3076,3 +3112,5 @@ const char *egsgpu_last_error(egsgpu_handle *h) { return h ? h->err.c_str() : "n
 void egsgpu_destroy(egsgpu_handle *h) { delete h; }
 
 }  // extern "C"
+
+#endif  // EGSGPU_PART_F64

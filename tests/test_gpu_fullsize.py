@@ -6,15 +6,14 @@ The parity tests compare with the oracle on reduced phantoms; here the full
 phantoms are checked through properties that do not depend on the number of
 histories:
   * FP64 history by history against the oracle for a few hundred histories.
-    Rounding differences between the GPU and the host compiler (fused
-    multiply-adds, last-ulp differences of log/exp) start at 1e-16; steps
-    limited by the distance to the nearest voxel face feed a position
-    difference into the next step length, so a 20 MeV electron track in 0.2 cm
-    voxels amplifies it by about 2% per step until, after hundreds of steps, a
-    branch decision flips and the history forks.  In 128^3 voxels about 10% of
-    the 20 MeV electron histories fork (0% in 0.8 cm voxels, 3% in 0.4 cm);
-    a forked history is as valid a sample as the oracle's, so the energy
-    deposited per history must still agree on average;
+    Neither side fuses multiply-adds, but log/exp can differ in the last ulp
+    between the GPU and the host; steps limited by the distance to the
+    nearest voxel face feed a position difference into the next step length,
+    so a 20 MeV electron track in 0.2 cm voxels amplifies it by about 2% per
+    step until a branch decision flips and the history forks.  In 128^3 voxels
+    about 3% of the 20 MeV electron histories fork (none in 0.4 or 0.8 cm
+    voxels); a forked history is as valid a sample as the oracle's, so the
+    energy deposited per history must still agree on average;
   * energy conservation of an FP32 run: deposited + escaped = source energy;
   * the tallies do not depend on how histories are chunked into wavefronts;
   * (c4) every phantom of the batched run equals a run of its own.
@@ -30,7 +29,7 @@ pytestmark = pytest.mark.gpu
 
 FULL = ["water30", "slab64", "water128e", "perturbed64"]
 NHIST = {"water30": 400, "slab64": 400, "water128e": 200, "perturbed64": 300}
-MATCH = {"water30": 0.97, "slab64": 0.97, "water128e": 0.8, "perturbed64": 0.97}
+MATCH = {"water30": 0.97, "slab64": 0.97, "water128e": 0.9, "perturbed64": 0.97}
 
 
 def engine(wl, precision, **cfg):

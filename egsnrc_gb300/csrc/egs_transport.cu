@@ -16,6 +16,8 @@
 //   k_batch     folds the batch tally into the per-voxel sum and sum of squares
 // Energy deposits are accumulated per thread while a particle stays in one
 // voxel and flushed with one FP64 atomic (tallies are L2-resident).
+// The file builds the FP32 engine and the C ABI; egs_transport_f64.cu builds
+// the FP64 engine from it (see EGSGPU_TU below).
 // Paths in comments are relative to the EGSnrc HEN_HOUSE directory.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>

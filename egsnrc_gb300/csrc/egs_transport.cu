@@ -2054,6 +2054,7 @@ struct Engine : EngineBase {
             if (events && (e = cudaEventRecord(gev[4 * r + 1], ws))) break;
             if (events && (e = cudaEventRecord(gev[4 * r + 2], ws))) break;
             if (hfl) k_electron<Real, false, false, true><<<ge, bs, 0, ws>>>(P);
+            else if (pi && multi) k_electron<Real, true, false, false, true><<<ge, bs, 0, ws>>>(P);
             else if (pi) k_electron<Real, false, false, false, true><<<ge, bs, 0, ws>>>(P);
             else if (adj) k_electron<Real, false, true><<<ge, bs, 0, ws>>>(P);
             else if (multi) k_electron<Real, true><<<ge, bs, 0, ws>>>(P);
@@ -2143,8 +2144,8 @@ struct Engine : EngineBase {
         if (hfl && (Multi || mode)) { err = "HOWFARLESS transport is for one homogeneous phantom (no adjoint)"; return EGSGPU_ERR_ARG; }
         if (hfl && !homogeneous) { err = "HOWFARLESS transport needs a homogeneous phantom"; return EGSGPU_ERR_ARG; }
         const bool pi = cfg.bca_algorithm == 1;
-        if (pi && (Multi || mode || hfl)) {
-            err = "PRESTA-I boundary crossing is for egsgpu_run (one phantom, no HOWFARLESS, no adjoint)";
+        if (pi && (mode || hfl)) {
+            err = "PRESTA-I boundary crossing is for egsgpu_run and egsgpu_run_phantoms (no HOWFARLESS, no adjoint)";
             return EGSGPU_ERR_ARG;
         }
         if (hfl) {
@@ -2152,8 +2153,8 @@ struct Engine : EngineBase {
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, false, false, true>, bs, 0));
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, false, false, true>, bs, 0));
         } else if (pi) {
-            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, false>, bs, 0));
-            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, false, false, false, true>, bs, 0));
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, Multi>, bs, 0));
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, Multi, false, false, true>, bs, 0));
         } else if (adj) {
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, false, true>, bs, 0));
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, false, true>, bs, 0));

@@ -70,8 +70,8 @@ typedef struct {
                              src/egsnrc.mortran:2782-2783, 1247-1345).  With
                              PRESTA-I a skindepth <= 1e-4 selects the old PRESTA
                              default from the lowest ECUT (:2794-2815).  PRESTA-I
-                             is for egsgpu_run only (one phantom, no HOWFARLESS,
-                             no adjoint, not egsgpu_run_noalloc). */
+                             is for egsgpu_run and egsgpu_run_phantoms (not with
+                             HOWFARLESS, the adjoint or egsgpu_run_noalloc). */
 } egsgpu_config;
 
 /* Source: egs++ EGS_ParallelBeam (sources/egs_parallel_beam) with a point

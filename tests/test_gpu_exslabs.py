@@ -108,3 +108,29 @@ def test_presta1_refused_where_it_has_no_kernel():
     e.close()
     with pytest.raises(eg.EGSError):
         eg.DoseEngine([W.WATER], bca_algorithm=2)
+
+
+def test_presta1_phantoms_match_separate_runs():
+    """PRESTA-I with several phantoms per run: each equals a run of its own."""
+    media = [W.WATER, W.LUNG, W.BONE]
+    ps = []
+    for k, (n, q, en) in enumerate(((10, -1, 4.0), (14, 0, 3.0))):
+        g = W.centred_geometry(n, 0.3, (np.arange(n ** 3) % 3).astype(np.int32))
+        src = eg.ParallelBeam(charge=q, energy=en, position=(0.0, 0.0, -1.0), rectangle=(-1, 1, -1, 1))
+        ps.append(dict(geometry=g, source=src, seed=31 + k, histories=600))
+    kw = dict(ecut=0.521, pcut=0.01, precision=64, bca_algorithm=1, skindepth=0.0)
+    e = eg.DoseEngine(media, **kw)
+    e.set_phantoms(ps)
+    e.run_phantoms(nbatch=2)
+    for k, p in enumerate(ps):
+        s, s2 = e.phantom_tallies(k)
+        one = eg.DoseEngine(media, **kw)
+        one.set_geometry(p["geometry"])
+        one.set_source(p["source"])
+        one.run(p["histories"], nbatch=2, seed=p["seed"])
+        r, r2, _ = one.tallies()
+        assert r.sum() > 0
+        assert np.allclose(s, r, rtol=1e-12, atol=1e-12 * r.max())
+        assert np.allclose(s2, r2, rtol=1e-12, atol=1e-12 * r2.max())
+        one.close()
+    e.close()

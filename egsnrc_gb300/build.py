@@ -36,7 +36,7 @@ def _newer(target, sources):
 
 
 def build_engine(force=False):
-    srcs = [os.path.join(CSRC, f) for f in ("egs_transport.cu", "egs_hatch.cpp", "egs_transport_f64.cu")]
+    srcs = [os.path.join(CSRC, f) for f in ("egs_transport.cu", "egs_hatch.cpp", "egs_transport_f64.cu", "egs_phsp.cpp")]
     deps = srcs + [os.path.join(CSRC, f) for f in ("egs_device.cuh", "egs_physics.cuh", "egs_hatch.h")] + [
         os.path.join(ROOT, "include", "egsgpu.h")]
     if not force and _newer(LIB, deps):
@@ -44,14 +44,15 @@ def build_engine(force=False):
     bdir = os.path.join(HERE, "_build")
     os.makedirs(bdir, exist_ok=True)
     objs = [os.path.join(bdir, "egs_transport.o"), os.path.join(bdir, "egs_hatch.o"),
-            os.path.join(bdir, "egs_transport_f64.o")]
+            os.path.join(bdir, "egs_transport_f64.o"), os.path.join(bdir, "egs_phsp.o")]
     cmds = [
         [NVCC] + ARCH + NVFLAGS + ["-c", srcs[0], "-o", objs[0]],
         ["g++", "-O2", "-std=c++17", "-fPIC", "-c", srcs[1], "-o", objs[1]],
         # the FP64 engine rounds like the CPU oracle: no fused multiply-adds
         [NVCC] + ARCH + NVFLAGS + ["--fmad=false", "-c", srcs[2], "-o", objs[2]],
+        ["g++", "-O2", "-std=c++17", "-fPIC", "-I" + os.path.join(ROOT, "include"), "-c", srcs[3], "-o", objs[3]],
     ]
-    with ThreadPoolExecutor(3) as ex:
+    with ThreadPoolExecutor(4) as ex:
         list(ex.map(_run, cmds))
     _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
     return LIB
@@ -73,6 +74,8 @@ def build_oracle(force=False):
     if force and os.path.exists(ORACLE_LIB):
         os.remove(ORACLE_LIB)
     _run(["make", "-s"], cwd=ORACLE_DIR)
+    # the reference's own IAEA phase-space library, where its sources are present
+    _run(["make", "-s", "ref"], cwd=ORACLE_DIR)
     return ORACLE_LIB
 
 

@@ -9,6 +9,7 @@
 // definition, MC transport parameter, rng definition, ausgab object
 // definition), the PEGS4 file is given with -p, and the dose goes to
 // <name>.3ddose in the egs_dose_scoring format.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -57,39 +58,63 @@ static bool planes(const Item *g, const char *p, const char *s, std::vector<doub
     return false;
 }
 
-// BEAMnrc phase-space file (egs++/sources/egs_phsp_source/egs_phsp_source.cpp:
-// header :64-130, records :360-423): "MODE0"/"MODE2", counts, energies, then
-// LATCH (bit 30 e-, bit 29 e+), E (total for charged, < 0 for a new history),
-// X, Y, U, V, WT (< 0 when W < 0) [, ZLAST].  Fills 7 floats per particle:
-// charge, kinetic energy, x, y, u, v, weight.
-static bool read_egsphsp(const std::string &path, std::vector<float> &out, double &incident, std::string &err) {
-    std::ifstream f(path, std::ios::binary);
-    if (!f) { err = "cannot open phase-space file " + path; return false; }
-    char mode[5];
-    f.read(mode, 5);
-    int rec = std::string(mode, 5) == "MODE0" ? 28 : (std::string(mode, 5) == "MODE2" ? 32 : 0);
-    if (!rec) { err = path + ": not an egsphsp file"; return false; }
-    int32_t n = 0, nphot = 0;
-    float ekmax = 0, ekmin = 0, ninc = 0;
-    f.read((char *)&n, 4); f.read((char *)&nphot, 4);
-    f.read((char *)&ekmax, 4); f.read((char *)&ekmin, 4); f.read((char *)&ninc, 4);
-    incident = ninc;
-    f.seekg(rec, std::ios::beg);
-    out.resize((size_t)n * 7);
-    std::vector<char> buf(rec);
-    for (int32_t i = 0; i < n; ++i) {
-        if (!f.read(buf.data(), rec)) { err = path + ": truncated"; return false; }
-        uint32_t latch;
-        float v[6];
-        std::memcpy(&latch, buf.data(), 4);
-        std::memcpy(v, buf.data() + 4, 24);
-        float q = (latch & (1u << 30)) ? -1.0f : ((latch & (1u << 29)) ? 1.0f : 0.0f);
-        double e = std::fabs(v[0]);
-        float *o = &out[(size_t)i * 7];
-        o[0] = q;
-        o[1] = (float)(q != 0 ? e - 0.5109989461 : e);
-        o[2] = v[1]; o[3] = v[2]; o[4] = v[3]; o[5] = v[4]; o[6] = v[5];
+// Phase-space sources: EGS_PhspSource (egs++/sources/egs_phsp_source/
+// egs_phsp_source.cpp:196-290 input, :364-470 reading and rejection) and
+// IAEA_PhspSource (egs++/sources/iaea_phsp_source/iaea_phsp_source.cpp:226-308
+// input, :310-470).  The file is read by egsgpu_read_phsp.  A rejected particle
+// keeps its place in the list with weight 0, as the reference hands it to the
+// application with wt = 0.  Rejection: the particle type ('particle type' =
+// electrons, photons, positrons, all or charged), the 'cutout' rectangle
+// (x_min x_max y_min y_max), the 'weight window' (wmin wmax) on the stored weight
+// divided by the number of uses (the sign of an egsphsp weight is the sign of w
+// and takes part, as in the reference), and, for egsphsp files, LATCH bit 31.
+// The IAEA source hands out LATCH 0, so bit 31 never rejects there.  Recycling
+// ('reuse photons/electrons', or 'recycle ...') must be the same number for
+// both.  Returns the plane z of the particles in *zplane.
+static bool load_phsp_source(const Item *s, bool iaea, std::vector<float> &phsp, int &recycle, double &zplane,
+                             std::string &err) {
+    const std::string path = s->get(iaea ? "iaea phase space file" : "phase space file");
+    egsgpu_phsp_info info;
+    if (egsgpu_read_phsp(path.c_str(), 0, 0, &info, nullptr, nullptr, nullptr)) {
+        err = egsgpu_last_error(nullptr);
+        return false;
     }
+    phsp.resize((size_t)info.n * 7);
+    std::vector<uint32_t> latch((size_t)info.n);
+    if (egsgpu_read_phsp(path.c_str(), 0, info.n, &info, phsp.data(), latch.data(), nullptr)) {
+        err = egsgpu_last_error(nullptr);
+        return false;
+    }
+    if (!(info.zmin == info.zmax)) {
+        err = path + ": the particles are not on one plane z = const";
+        return false;
+    }
+    zplane = info.zmin;
+    const std::string pt = egsin::norm(s->get("particle type", "all"));
+    const int want = pt == "photons" ? 0 : pt == "electrons" ? -1 : pt == "positrons" ? 1 : pt == "charged" ? 2 : 3;
+    if (want == 3 && pt != "all") { err = "unknown particle type '" + pt + "'"; return false; }
+    auto cut = Item::numbers(s->get("cutout", ""));
+    auto win = Item::numbers(s->get("weight window", ""));
+    auto rec = [&](const std::string &what) {   // 'reuse ...', else 'recycle ...'
+        return (int)std::max(0.0, s->num("reuse " + what, s->num("recycle " + what, 0)));
+    };
+    const int rp = rec("photons"), re = rec("electrons");
+    if (rp != re) { err = "different recycle numbers for photons and electrons are not supported"; return false; }
+    recycle = rp;
+    for (size_t i = 0, k = 0; i < phsp.size(); i += 7, ++k) {
+        const float q = phsp[i];
+        bool keep = want == 3 || (want == 2 ? q != 0 : q == (float)want);
+        if (cut.size() == 4 && (phsp[i + 2] < cut[0] || phsp[i + 2] > cut[1] || phsp[i + 3] < cut[2] ||
+                                phsp[i + 3] > cut[3]))
+            keep = false;
+        if (win.size() == 2) {
+            const double wt = (iaea ? std::fabs(phsp[i + 6]) : phsp[i + 6]) / (recycle + 1.0);
+            if (wt < win[0] || wt > win[1]) keep = false;
+        }
+        if (!iaea && (latch[k] & 0x80000000u)) keep = false;
+        if (!keep) phsp[i + 6] = phsp[i + 6] < 0 ? -0.0f : 0.0f;
+    }
+    std::printf("phase space: %lld particles, %.0f incident histories\n", info.n, info.incident);
     return true;
 }
 
@@ -286,34 +311,18 @@ int main(int argc, char **argv) {
     }
     std::vector<float> phsp;
     std::string lib = egsin::norm(s->get("library"));
-    if (lib == "egs_phsp_source") {
-        // EGS_PhspSource (egs_phsp_source.cpp:196-280): particle type, cutout
-        // and recycling; rejected particles keep their place with weight 0
-        double incident = 0;
+    if (lib == "egs_phsp_source" || lib == "iaea_phsp_source") {
+        double zplane = 0;
         std::string perr;
-        if (!read_egsphsp(s->get("phase space file"), phsp, incident, perr)) return fail(perr);
-        std::string pt = egsin::norm(s->get("particle type", "all"));
-        int want = pt == "photons" ? 0 : pt == "electrons" ? -1 : pt == "positrons" ? 1 : pt == "charged" ? 2 : 3;
-        if (want == 3 && pt != "all") return fail("unknown particle type '" + pt + "'");
-        auto cut = Item::numbers(s->get("cutout", ""));
-        int rp = (int)s->num("recycle photons", 0), re = (int)s->num("recycle electrons", 0);
-        if (rp != re) return fail("different recycle numbers for photons and electrons are not supported");
-        for (size_t i = 0; i < phsp.size(); i += 7) {
-            float q = phsp[i];
-            bool keep = want == 3 || (want == 2 ? q != 0 : q == (float)want);
-            if (cut.size() == 4 && (phsp[i + 2] < cut[0] || phsp[i + 2] > cut[1] || phsp[i + 3] < cut[2] ||
-                                    phsp[i + 3] > cut[3]))
-                keep = false;
-            if (!keep) phsp[i + 6] = phsp[i + 6] < 0 ? -0.0f : 0.0f;
-        }
+        if (!load_phsp_source(s, lib == "iaea_phsp_source", phsp, src.recycle, zplane, perr)) return fail(perr);
         src.shape = 2;
         src.nphsp = (long long)(phsp.size() / 7);
         src.phsp = phsp.data();
-        src.recycle = rp;
         for (int k = 0; k < 3; ++k) src.pos[k] = shift[k];
+        src.pos[2] += zplane;
         src.dir[2] = 1;
-        std::printf("phase space: %lld particles, %.0f incident histories\n", src.nphsp, incident);
-    } else if (lib != "egs_parallel_beam") return fail("only egs_parallel_beam and egs_phsp_source sources are supported");
+    } else if (lib != "egs_parallel_beam")
+        return fail("only egs_parallel_beam, egs_phsp_source and iaea_phsp_source sources are supported");
     if (lib == "egs_parallel_beam") {
     src.charge = (int)s->num("charge", 0);
     auto dir = Item::numbers(s->get("direction", "0 0 1"));

@@ -3078,6 +3078,10 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[(size_t)EGSGPU_
 static std::mutex g_noalloc_mutex;
 static unsigned char *g_noalloc_addr[256] = {};
 
+namespace egsgpu_host {
+const char *host_error();   // egs_phsp.cpp: last error of a host-only call on this thread
+}
+
 extern "C" {
 
 int egsgpu_run_noalloc(egsgpu_handle *h, long long first, long long n, uint32_t seed, double *dose, void *stream) {
@@ -3110,7 +3114,7 @@ int egsgpu_run_noalloc(egsgpu_handle *h, long long first, long long n, uint32_t 
                                (size_t)EGSGPU_NOALLOC_SCRATCH_MIB << 20, h->err);
 }
 
-const char *egsgpu_last_error(egsgpu_handle *h) { return h ? h->err.c_str() : "null handle"; }
+const char *egsgpu_last_error(egsgpu_handle *h) { return h ? h->err.c_str() : egsgpu_host::host_error(); }
 
 void egsgpu_destroy(egsgpu_handle *h) { delete h; }
 

@@ -15,6 +15,15 @@
   record per particle: LATCH (bit 30 electron, bit 29 positron), E (total
   energy for charged particles; negative for the first particle of a new
   incident history), X, Y, U, V, WT (negative when W < 0) and, in MODE2, ZLAST.
+* IAEA phase-space files (the input of egs++ IAEA_PhspSource,
+  egs++/sources/iaea_phsp_source/iaea_phsp_source.cpp:77-224, :310-417; format
+  HEN_HOUSE/iaea_phsp/iaea_header.cpp:60-330 and :700-800, iaea_record.cpp:85-230):
+  a text header <name>.IAEAheader of "$KEYWORD:" blocks and binary records in
+  <name>.IAEAphsp.  A record holds the particle type as a signed byte (1
+  photon, 2 e-, 3 e+; negative when W < 0), the kinetic energy (negative for a
+  new history), the stored ones of X Y Z U V WEIGHT (RECORD_CONTENTS; the rest
+  are RECORD_CONSTANT values), extra floats and extra int32s (type 1 the
+  incremental history number, type 2 the EGS LATCH).
 """
 import numpy as np
 
@@ -178,3 +187,173 @@ def write_egsphsp(path, particles, incident, new_history=None, mode="MODE0", rm=
     with open(path, "wb") as f:
         f.write(bytes(hdr))
         f.write(r.tobytes())
+
+
+IAEA_KEYS = ("X", "Y", "Z", "U", "V", "W", "Weight")
+
+
+def _iaea_blocks(text):
+    """The "$KEY:" blocks of an IAEA header, comments removed, blank lines skipped."""
+    import re
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    blocks, cur = {}, None
+    for line in text.splitlines():
+        line = line.strip()
+        if not line:
+            continue
+        if line.startswith("$") and ":" in line:
+            cur = blocks.setdefault(line[1:line.index(":")], [])
+            continue
+        if cur is not None:
+            cur.append(line)
+    return blocks
+
+
+def _iaea_base(path):
+    p = str(path)
+    for ext in (".IAEAheader", ".IAEAphsp"):
+        if p.endswith(ext):
+            return p[:-len(ext)]
+    return p
+
+
+def read_iaea_phsp(path):
+    """Returns (particles, header) like read_egsphsp for an IAEA phase-space
+    pair (path = <name>, with or without either extension); header has mode
+    "IAEA", n, photons, incident, z (the constant Z, or the array of stored
+    Z), latch (zeros if none is stored) and new_history."""
+    base = _iaea_base(path)
+    with open(base + ".IAEAheader") as f:
+        B = _iaea_blocks(f.read())
+    contents = [int(float(v.split()[0])) for v in B["RECORD_CONTENTS"]]
+    nxf, nxl = contents[7], contents[8]
+    ftypes = contents[9:9 + nxf]
+    ltypes = contents[9 + nxf:9 + nxf + nxl]
+    const = {}
+    vals = iter(B.get("RECORD_CONSTANT", []))
+    for i, k in enumerate(IAEA_KEYS):
+        if contents[i] <= 0:
+            const[k] = float(next(vals).split()[0])
+    order = int(B["BYTE_ORDER"][0].split()[0])
+    end = "<" if order == 1234 else ">"
+    fields = [("type", "i1"), ("e", end + "f4")]
+    fields += [(k, end + "f4") for i, k in enumerate(IAEA_KEYS) if i != 5 and contents[i] > 0]
+    fields += [("xf%d" % j, end + "f4") for j in range(nxf)]
+    fields += [("xl%d" % j, end + "i4") for j in range(nxl)]
+    dt = np.dtype(fields)
+    n = int(float(B["PARTICLES"][0].split()[0]))
+    raw = np.fromfile(base + ".IAEAphsp", dtype=np.uint8)
+    if raw.size != n * dt.itemsize or int(float(B["CHECKSUM"][0].split()[0])) != raw.size:
+        raise ValueError("%s: file size does not match the header" % base)
+    r = np.frombuffer(raw.tobytes(), dtype=dt)
+    t = r["type"].astype(np.int32)
+    wneg = t < 0
+    t = np.abs(t)
+    if np.any((t < 1) | (t > 3)):
+        raise ValueError("%s: records other than photons, electrons and positrons" % base)
+    col = {k: (r[k].astype(np.float32) if k in r.dtype.names else np.full(n, const[k], dtype=np.float32))
+           for i, k in enumerate(IAEA_KEYS) if i != 5}
+    u, v = col["U"].copy(), col["V"].copy()
+    if contents[5] > 0:
+        aux = u * u + v * v                       # float32, as the record reader forms it
+        big = aux.astype(np.float64) > 1.0
+        s = np.sqrt(aux[big])
+        u[big] /= s
+        v[big] /= s
+        w = np.where(big, np.float32(0), np.sqrt((1.0 - aux.astype(np.float64)).clip(0).astype(np.float32)))
+        w = np.where(wneg, -w, w)
+    else:
+        w = np.full(n, const["W"], dtype=np.float32)
+    q = np.where(t == 1, 0, np.where(t == 2, -1, 1)).astype(np.float32)
+    wt = np.abs(col["Weight"])
+    wt = np.where((w < 0) | ((w == 0) & wneg), -wt, wt)
+    parts = np.stack([q, np.abs(r["e"]).astype(np.float32), col["X"], col["Y"], u, v, wt], axis=1).astype(np.float32)
+    newh = r["e"] < 0
+    latch = np.zeros(n, dtype=np.uint32)
+    for j, lt in enumerate(ltypes):
+        if lt == 1:
+            newh = r["xl%d" % j] > 0
+        if lt == 2:
+            latch = r["xl%d" % j].astype(np.uint32)
+    hdr = dict(mode="IAEA", n=n, photons=int(float(B["PHOTONS"][0].split()[0])) if "PHOTONS" in B else 0,
+               incident=float(B["ORIG_HISTORIES"][0].split()[0]) if "ORIG_HISTORIES" in B else 0.0,
+               z=col["Z"] if contents[2] > 0 else const["Z"], latch=latch, new_history=newh,
+               extra_float_types=ftypes, extra_long_types=ltypes)
+    return parts, hdr
+
+
+def write_iaea_phsp(path, particles, incident, new_history=None, z=0.0, latch=None, constant=(),
+                    byte_order="little", pcut=0.0, ecut=0.0, code="egsnrc_gb300"):
+    """Writes particles ({charge, kinetic energy, x, y, u, v, weight} rows, a
+    negative weight meaning w < 0) as an IAEA phase-space pair <path>.IAEAheader
+    and <path>.IAEAphsp.  z is the plane (a constant) or an array stored per
+    particle; quantities named in `constant` (of X, Y, U, V, Weight) are
+    written once in RECORD_CONSTANT from the first particle; latch, when given,
+    is stored as an EGS LATCH extra int32.  pcut and ecut (kinetic, MeV) are
+    the header's global photon and particle energy cutoffs."""
+    base = _iaea_base(path)
+    p = np.asarray(particles, dtype=np.float32).reshape(-1, 7)
+    n = len(p)
+    wneg = p[:, 6] < 0
+    z_arr = np.ndim(z) > 0
+    cols = {"X": p[:, 2], "Y": p[:, 3], "Z": np.asarray(z, dtype=np.float32) if z_arr else None,
+            "U": p[:, 4], "V": p[:, 5], "Weight": np.abs(p[:, 6])}
+    stored = {k: (k == "Z" and z_arr) or (k != "Z" and k not in constant) for k in cols}
+    contents = [int(stored["X"]), int(stored["Y"]), int(stored["Z"]), int(stored["U"]), int(stored["V"]), 1,
+                int(stored["Weight"]), 0, 1 if latch is not None else 0]
+    end = "<" if byte_order == "little" else ">"
+    fields = [("type", "i1"), ("e", end + "f4")] + [(k, end + "f4") for k in ("X", "Y", "Z", "U", "V", "Weight")
+                                                     if stored[k]]
+    if latch is not None:
+        fields.append(("xl0", end + "i4"))
+    r = np.zeros(n, dtype=np.dtype(fields))
+    t = np.where(p[:, 0] == 0, 1, np.where(p[:, 0] < 0, 2, 3)).astype(np.int8)
+    r["type"] = np.where(wneg, -t, t)
+    e = p[:, 1]
+    r["e"] = np.where(new_history, -e, e) if new_history is not None else e
+    for k in ("X", "Y", "Z", "U", "V", "Weight"):
+        if stored[k]:
+            r[k] = cols[k]
+    if latch is not None:
+        r["xl0"] = np.asarray(latch).astype(np.uint32).view(np.int32)
+    with open(base + ".IAEAphsp", "wb") as f:
+        f.write(r.tobytes())
+    kinds = [(1, "PHOTONS"), (2, "ELECTRONS"), (3, "POSITRONS")]
+    L = ["$IAEA_INDEX:", "0", "", "$TITLE:", "phase space", "", "$FILE_TYPE:", "0", "",
+         "$CHECKSUM:", "%d" % (n * r.dtype.itemsize), "", "$RECORD_CONTENTS:"]
+    L += ["   %d     // %s is stored ?" % (c, k) for c, k in zip(contents[:7], IAEA_KEYS)]
+    L += ["   %d     // Extra floats stored ?" % contents[7], "   %d     // Extra longs stored ?" % contents[8]]
+    if latch is not None:
+        L.append("   2     // LATCH EGS variable stored in the extralong array [ 0]")
+    L += ["", "$RECORD_CONSTANT:"]
+    for k in IAEA_KEYS:
+        if k == "Z" and not z_arr:
+            L.append("   %.9g     // Constant Z" % float(z))
+        elif k in constant:
+            L.append("   %.9g     // Constant %s" % (float(cols[k][0]), k))
+    L += ["", "$RECORD_LENGTH:", "%d" % r.dtype.itemsize, "", "$BYTE_ORDER:",
+          "1234" if byte_order == "little" else "4321", "",
+          "$ORIG_HISTORIES:", "%d" % int(incident), "", "$PARTICLES:", "%d" % n, ""]
+    for kind, name in kinds:
+        m = int((t == kind).sum())
+        if m:
+            L += ["$%s:" % name, "%d" % m, ""]
+    # every mandatory block carries a line: the reference reader refuses an empty one
+    L += ["$TRANSPORT_PARAMETERS:", "-", "", "$MACHINE_TYPE:", "-", "", "$MONTE_CARLO_CODE_VERSION:", code, "",
+          "$GLOBAL_PHOTON_ENERGY_CUTOFF:", " %.5f" % pcut, "", "$GLOBAL_PARTICLE_ENERGY_CUTOFF:", " %.5f" % ecut, "",
+          "$COORDINATE_SYSTEM_DESCRIPTION:", "-", "", "$STATISTICAL_INFORMATION_PARTICLES:",
+          "//        Weight        Wmin       Wmax       <E>         Emin         Emax    Particle"]
+    for kind, name in kinds:
+        m = t == kind
+        if m.any():
+            w_, e_ = np.abs(p[m, 6]).astype(np.float64), p[m, 1].astype(np.float64)
+            L.append("  %.6g  %.6g  %.6g  %.6g  %.6g  %.6g  %s" % (w_.sum(), w_.min(), w_.max(),
+                                                                  (w_ * e_).sum() / w_.sum(), e_.min(), e_.max(),
+                                                                  name))
+    L += ["", "$STATISTICAL_INFORMATION_GEOMETRY:"]
+    for k in ("X", "Y", "Z"):
+        if stored[k]:
+            L.append(" %.6g  %.6g" % (float(np.min(cols[k])), float(np.max(cols[k]))))
+    with open(base + ".IAEAheader", "w") as f:
+        f.write("\n".join(L) + "\n")

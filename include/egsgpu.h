@@ -261,7 +261,40 @@ int egsgpu_restore(egsgpu_handle *h, const void *buf, size_t size);
 int egsgpu_run_noalloc(egsgpu_handle *h, long long first, long long n, uint32_t seed, double *dose,
                        void *stream);
 
-/* Last error message of the handle (never NULL). */
+/* Phase-space files, the particle input of egs++ EGS_PhspSource and
+ * IAEA_PhspSource and of DOSXYZnrc isource 2 (host only: needs no GPU and no
+ * handle).  Reads the header, and records [first, first+count), of
+ *   - a BEAMnrc .egsphsp file, MODE0 or MODE2
+ *     (egs++/sources/egs_phsp_source/egs_phsp_source.cpp:77-160 header,
+ *     :364-423 records), or
+ *   - an IAEA phase-space pair <name>.IAEAheader + <name>.IAEAphsp
+ *     (egs++/sources/iaea_phsp_source/iaea_phsp_source.cpp:77-224, :310-417;
+ *     HEN_HOUSE/iaea_phsp/iaea_header.cpp:60-330, iaea_record.cpp:145-230);
+ *     `path` is <name>, with or without either extension.
+ * Each particle becomes the 7 floats egsgpu_source.phsp takes: charge,
+ * kinetic energy (MeV), x, y, u, v, weight (negative when w < 0).
+ * `particles` (7*count floats), `latch` (count; 0 where the file stores no
+ * LATCH) and `new_history` (count; 1 for the first particle of an incident
+ * history) may each be NULL; count = 0 reads the header only.  Files written
+ * with the other byte order are read.  A file whose size disagrees with its
+ * header, or an IAEA record of a neutron or proton, is EGSGPU_ERR_DATA.  The
+ * message of a failed call is egsgpu_last_error(NULL) on the same thread. */
+typedef struct egsgpu_phsp_info {
+    int format;          /* 0 egsphsp MODE0, 1 egsphsp MODE2, 2 IAEA             */
+    int has_latch;       /* the records carry an EGS LATCH                       */
+    long long n;         /* particles in the file                                */
+    long long photons;   /* photons in the file                                  */
+    double incident;     /* incident histories that made the file                */
+    double ekmax;        /* maximum kinetic energy (MeV); 0 if the header has none */
+    double zmin, zmax;   /* z of the records read: 0 for egsphsp (the scoring
+                            plane); for IAEA the constant Z, or the range of the
+                            stored Z (NaN when only the header was read)       */
+} egsgpu_phsp_info;
+int egsgpu_read_phsp(const char *path, long long first, long long count, egsgpu_phsp_info *info,
+                     float *particles, uint32_t *latch, unsigned char *new_history);
+
+/* Last error message of the handle (never NULL); with a NULL handle, the
+ * last error of a host-only call (egsgpu_read_phsp) on this thread. */
 const char *egsgpu_last_error(egsgpu_handle *h);
 
 void egsgpu_destroy(egsgpu_handle *h);

@@ -163,6 +163,55 @@ def test_app_phase_space_source_matches_binding(tmp_path):
     compare(dose_file, eng.dose()[0])
 
 
+def ex16_particles(tmp_path):
+    path = tmp_path / "EX16MVp.egsphsp1"
+    with gzip.open(os.path.join(HERE, "golden", "EX16MVp.egsphsp1.gz"), "rb") as a, open(path, "wb") as b:
+        shutil.copyfileobj(a, b)
+    p, hdr = formats.read_egsphsp(str(path))
+    return path, p, hdr
+
+
+def binding_dose(p, recycle=1):
+    b = -15 + 2.0 * np.arange(16)
+    eng = eg.DoseEngine([W.WATER], ecut=0.7, pcut=0.01)
+    eng.set_geometry(eg.XYZGeometry(b, b, 2.0 * np.arange(16), 0))
+    eng.set_source(eg.PhaseSpaceSource(p, position=(0, 0, -0.5), recycle=recycle))
+    eng.run(30000, nbatch=3, seed=3)
+    return eng.dose()[0]
+
+
+def test_app_iaea_phase_space_source_matches_binding(tmp_path):
+    """iaea_phsp_source: the EX16MVp particles written as an IAEA file on the
+    plane z = 0.25 and moved by -0.75 cm give the dose of the same particles
+    placed at z = -0.5 through the binding."""
+    _, p, hdr = ex16_particles(tmp_path)
+    base = tmp_path / "ex16"
+    formats.write_iaea_phsp(str(base), p, hdr["incident"], new_history=hdr["new_history"], z=0.25)
+    text = PHSP.replace("egs_phsp_source", "iaea_phsp_source").replace("phase space file = PHSPFILE",
+                                                                       "iaea phase space file = " + str(base))
+    text = text.replace("recycle photons", "reuse photons").replace("recycle electrons", "reuse electrons")
+    text = text.replace("translation = 0 0 -0.5", "translation = 0 0 -0.75")
+    dose_file, _ = run_app(tmp_path, text, "iaea")
+    compare(dose_file, binding_dose(p))
+
+
+def test_app_phase_space_selection_matches_binding(tmp_path):
+    """'particle type', 'cutout' and 'weight window' of egs_phsp_source: the
+    rejected particles carry weight 0, the rest are transported unchanged."""
+    path, p, _ = ex16_particles(tmp_path)
+    text = PHSP.replace("PHSPFILE", str(path)).replace("particle type = all", "particle type = photons\n"
+                                                       "        cutout = -4 4 -3 5\n"
+                                                       "        weight window = 0.0001 0.0249")
+    dose_file, _ = run_app(tmp_path, text, "phsp_sel")
+    q = p.copy()
+    wt = q[:, 6].astype(np.float64) / 2.0   # the stored weight over the two uses of each particle
+    keep = (q[:, 0] == 0) & (q[:, 2] >= -4) & (q[:, 2] <= 4) & (q[:, 3] >= -3) & (q[:, 3] <= 5)
+    keep &= (wt >= 0.0001) & (wt <= 0.0249)
+    assert 100 < keep.sum() < len(q) - 100
+    q[~keep, 6] = np.where(q[~keep, 6] < 0, -0.0, 0.0)
+    compare(dose_file, binding_dose(q))
+
+
 def test_app_presta1_and_smax_match_binding(tmp_path):
     """The transport keys "Boundary crossing algorithm = PRESTA-I", "Skin
     depth for BCA" and "Global Smax" reach the engine as the binding sets them."""

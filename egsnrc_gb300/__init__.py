@@ -187,6 +187,19 @@ class PhaseSpaceSource:
         self.s.energy = float(self._p[:, 1].max())
         self.s.charge = -1 if np.any(self._p[:, 0] != 0) else 0
 
+    @classmethod
+    def from_file(cls, path, shift=(0.0, 0.0, 0.0), recycle=0):
+        """The particles of an egsphsp or IAEA file (read_phase_space), on the
+        file's plane (z = 0 for egsphsp, the IAEA constant Z) moved by shift,
+        as egs_transformed_source with a translation moves them."""
+        p, info = read_phase_space(path)
+        if not info["zmin"] == info["zmax"]:
+            raise ValueError("%s: the particles are not on one plane z = const" % path)
+        pos = (shift[0], shift[1], shift[2] + info["zmin"])
+        src = cls(p, position=pos, recycle=recycle)
+        src.info = info
+        return src
+
 
 PHSP_FORMATS = {0: "MODE0", 1: "MODE2", 2: "IAEA"}
 

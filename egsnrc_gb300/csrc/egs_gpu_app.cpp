@@ -65,9 +65,10 @@ static bool planes(const Item *g, const char *p, const char *s, std::vector<doub
 // keeps its place in the list with weight 0, as the reference hands it to the
 // application with wt = 0.  Rejection: the particle type ('particle type' =
 // electrons, photons, positrons, all or charged), the 'cutout' rectangle
-// (x_min x_max y_min y_max), the 'weight window' (wmin wmax) on the stored weight
-// divided by the number of uses (the sign of an egsphsp weight is the sign of w
-// and takes part, as in the reference), and, for egsphsp files, LATCH bit 31.
+// (x_min x_max y_min y_max), the 'weight window' (wmin wmax) on the stored
+// weight divided by the number of uses (the sign of an egsphsp weight is the
+// sign of w and takes part, as in the reference), and, for egsphsp files,
+// LATCH bit 31 and the LATCH filter.
 // The IAEA source hands out LATCH 0, so bit 31 never rejects there.  Recycling
 // ('reuse photons/electrons', or 'recycle ...') must be the same number for
 // both.  Returns the plane z of the particles in *zplane.
@@ -101,6 +102,31 @@ static bool load_phsp_source(const Item *s, bool iaea, std::vector<float> &phsp,
     const int rp = rec("photons"), re = rec("electrons");
     if (rp != re) { err = "different recycle numbers for photons and electrons are not supported"; return false; }
     recycle = rp;
+    // LATCH filter (egs_phsp_source.cpp:226-252, :446-518): 'filter type = 0' with
+    // 'latch setting = b1 b2', two strings of 0/1 for LATCH bits 0, 1, ...: a particle
+    // is rejected unless it has one of the bits set to 1 in b1 (when b1 has any), or
+    // when it has one of the bits set to 1 in b2, which count on from where b1 ends.
+    // More than 29 bits in all leaves the filter off, as in the reference.
+    uint32_t filter1 = 0, filter2 = 0;
+    if (s->has("filter type") && s->has("latch setting")) {
+        const auto ft = Item::numbers(s->get("filter type"));
+        const auto ls = Item::words(s->get("latch setting"));
+        if (!ft.empty() && ft[0] != 0) {
+            err = "only 'filter type = 0' is supported (types 1-3 set no filter bits in egs++ either)";
+            return false;
+        }
+        if (iaea) {
+            err = "LATCH filters need the egsphsp LATCH: IAEA_PhspSource hands out LATCH 0";
+            return false;
+        }
+        const std::string b1 = ls.size() > 0 ? ls[0] : "", b2 = ls.size() > 1 ? ls[1] : "";
+        if (b1.size() + b2.size() <= 29) {
+            for (size_t i = 0; i < b1.size(); ++i)
+                if (b1[i] == '1') filter1 |= 1u << i;
+            for (size_t j = 0; j < b2.size(); ++j)
+                if (b2[j] == '1') filter2 |= 1u << (b1.size() + j);
+        }
+    }
     for (size_t i = 0, k = 0; i < phsp.size(); i += 7, ++k) {
         const float q = phsp[i];
         bool keep = want == 3 || (want == 2 ? q != 0 : q == (float)want);
@@ -112,6 +138,7 @@ static bool load_phsp_source(const Item *s, bool iaea, std::vector<float> &phsp,
             if (wt < win[0] || wt > win[1]) keep = false;
         }
         if (!iaea && (latch[k] & 0x80000000u)) keep = false;
+        if ((filter1 && !(latch[k] & filter1)) || (latch[k] & filter2)) keep = false;
         if (!keep) phsp[i + 6] = phsp[i + 6] < 0 ? -0.0f : 0.0f;
     }
     std::printf("phase space: %lld particles, %.0f incident histories\n", info.n, info.incident);

@@ -212,6 +212,23 @@ def test_app_phase_space_selection_matches_binding(tmp_path):
     compare(dose_file, binding_dose(q))
 
 
+def test_app_latch_filter_matches_binding(tmp_path):
+    """'filter type = 0' with 'latch setting = 0011 000000001': keep particles
+    with LATCH bit 2 or 3, reject those with bit 4 + 8 = 12."""
+    path, p, _ = ex16_particles(tmp_path)
+    text = PHSP.replace("PHSPFILE", str(path)).replace("particle type = all", "particle type = all\n"
+                                                       "        filter type = 0\n"
+                                                       "        latch setting = 0011 000000001")
+    dose_file, _ = run_app(tmp_path, text, "phsp_latch")
+    _, info = eg.read_phase_space(str(path))
+    latch = info["latch"]
+    keep = ((latch & 0b1100) != 0) & ((latch & (1 << 12)) == 0) & ((latch >> 31) == 0)
+    assert 100 < keep.sum() < len(p) - 100
+    q = p.copy()
+    q[~keep, 6] = np.where(q[~keep, 6] < 0, -0.0, 0.0)
+    compare(dose_file, binding_dose(q))
+
+
 def test_app_presta1_and_smax_match_binding(tmp_path):
     """The transport keys "Boundary crossing algorithm = PRESTA-I", "Skin
     depth for BCA" and "Global Smax" reach the engine as the binding sets them."""

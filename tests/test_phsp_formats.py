@@ -105,6 +105,22 @@ def test_iaea_constants_stored_z_and_direction_edge(tmp_path):
     assert np.isnan(h0["zmin"])
 
 
+def test_phase_space_source_from_file(tmp_path, ex16):
+    """PhaseSpaceSource.from_file: the same particles from either format, on the
+    file's plane moved by the shift; particles on several planes refused."""
+    path, p, hdr, _ = ex16
+    base = str(tmp_path / "plane")
+    F.write_iaea_phsp(base, p, hdr["incident"], z=0.25)
+    a = eg.PhaseSpaceSource.from_file(path, shift=(1.0, 0.0, -0.5), recycle=2)
+    b = eg.PhaseSpaceSource.from_file(base, shift=(1.0, 0.0, -0.75), recycle=2)
+    assert np.array_equal(a._p, p) and np.array_equal(b._p, p)
+    assert tuple(a.s.pos) == tuple(b.s.pos) == (1.0, 0.0, -0.5) and a.s.recycle == b.s.recycle == 2
+    assert a.s.nphsp == b.s.nphsp == len(p) and a.info["format"] == "MODE2" and b.info["format"] == "IAEA"
+    F.write_iaea_phsp(base, p[:3], 1, z=np.array([0.0, 1.0, 2.0], dtype=np.float32))
+    with pytest.raises(ValueError):
+        eg.PhaseSpaceSource.from_file(base)
+
+
 def test_iaea_refusals(tmp_path, ex16):
     _, p, hdr, _ = ex16
     base = str(tmp_path / "bad")

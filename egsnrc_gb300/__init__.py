@@ -7,6 +7,7 @@ ABI declared in include/egsgpu.h.  The engine library must be built
 it raises instead of falling back to anything else.
 """
 import ctypes as C
+import math
 import os
 
 import numpy as np
@@ -41,7 +42,8 @@ class SourceStruct(C.Structure):
                 ("xmax", C.c_double), ("ymin", C.c_double), ("ymax", C.c_double), ("dir", C.c_double * 3),
                 ("spectrum", C.c_int), ("energy", C.c_double), ("nbins", C.c_int),
                 ("edges", C.POINTER(C.c_double)), ("weights", C.POINTER(C.c_double)),
-                ("nphsp", C.c_longlong), ("phsp", C.POINTER(C.c_float)), ("recycle", C.c_int)]
+                ("nphsp", C.c_longlong), ("phsp", C.POINTER(C.c_float)), ("recycle", C.c_int),
+                ("rot", C.c_double * 9)]
 
 
 class PhspInfo(C.Structure):
@@ -175,7 +177,7 @@ class PhaseSpaceSource:
     position[0], position[1].  Each particle is used recycle + 1 times with
     its weight shared."""
 
-    def __init__(self, particles, position=(0.0, 0.0, 0.0), recycle=0):
+    def __init__(self, particles, position=(0.0, 0.0, 0.0), recycle=0, rotation=None):
         self._p = np.ascontiguousarray(particles, dtype=np.float32).reshape(-1, 7)
         self.s = SourceStruct()
         self.s.shape = 2
@@ -186,50 +188,87 @@ class PhaseSpaceSource:
         self.s.recycle = int(recycle)
         self.s.energy = float(self._p[:, 1].max())
         self.s.charge = -1 if np.any(self._p[:, 0] != 0) else 0
+        if rotation is not None:
+            self.s.rot[:] = tuple(float(v) for v in np.asarray(rotation, dtype=np.float64).reshape(9))
 
     @classmethod
-    def from_file(cls, path, shift=(0.0, 0.0, 0.0), recycle=0):
+    def from_file(cls, path, shift=(0.0, 0.0, 0.0), recycle=0, rotation=None):
         """The particles of an egsphsp or IAEA file (read_phase_space), on the
-        file's plane (z = 0 for egsphsp, the IAEA constant Z) moved by shift,
-        as egs_transformed_source with a translation moves them."""
+        file's plane (z = 0 for egsphsp, the IAEA constant Z), rotated by
+        `rotation` and moved by shift, as egs_transformed_source moves them."""
         p, info = read_phase_space(path)
         if not info["zmin"] == info["zmax"]:
             raise ValueError("%s: the particles are not on one plane z = const" % path)
-        pos = (shift[0], shift[1], shift[2] + info["zmin"])
-        src = cls(p, position=pos, recycle=recycle)
+        R = np.eye(3) if rotation is None else np.asarray(rotation, dtype=np.float64).reshape(3, 3)
+        # the file's plane z0: R (x, y, z0) + shift = R (x, y, 0) + (shift + z0 R e_z)
+        t = np.asarray(shift, dtype=np.float64) + info["zmin"] * R[:, 2]
+        src = cls(p, position=tuple(t), recycle=recycle, rotation=rotation)
         src.info = info
         return src
 
 
-PHSP_FORMATS = {0: "MODE0", 1: "MODE2", 2: "IAEA"}
+def _mul(A, B):
+    # row-by-column sums in the order egs++ forms them (egs_transformations.h:251-259)
+    return [[A[i][0] * B[0][j] + A[i][1] * B[1][j] + A[i][2] * B[2][j] for j in range(3)] for i in range(3)]
 
 
-def read_phase_space(path, first=0, count=None):
-    """Reads a phase-space file through the library's reader (egsgpu_read_phsp;
-    host only, no GPU): a BEAMnrc .egsphsp file or an IAEA pair
-    <name>.IAEAheader + <name>.IAEAphsp (path = <name>, with or without either
-    extension).  Returns (particles, info): particles an (count, 7) float32
-    array of {charge, kinetic energy, x, y, u, v, weight} as PhaseSpaceSource
-    takes them; info a dict with format, n, photons, incident, ekmax, zmin,
-    zmax, has_latch, latch and new_history (arrays over the records read)."""
-    L = load_library()
-    info = PhspInfo()
-    p = str(path).encode()
-    rc = L.egsgpu_read_phsp(p, 0, 0, C.byref(info), None, None, None)
-    if rc:
-        raise EGSError(rc, L.egsgpu_last_error(None).decode())
-    n = info.n - first if count is None else count
-    parts = np.zeros((max(n, 0), 7), dtype=np.float32)
-    latch = np.zeros(max(n, 0), dtype=np.uint32)
-    newh = np.zeros(max(n, 0), dtype=np.uint8)
-    rc = L.egsgpu_read_phsp(p, first, n, C.byref(info), parts.ctypes.data_as(C.POINTER(C.c_float)),
-                            latch.ctypes.data_as(C.POINTER(C.c_uint32)), newh.ctypes.data_as(C.POINTER(C.c_ubyte)))
-    if rc:
-        raise EGSError(rc, L.egsgpu_last_error(None).decode())
-    out = dict(format=PHSP_FORMATS[info.format], n=info.n, photons=info.photons, incident=info.incident,
-               ekmax=info.ekmax, zmin=info.zmin, zmax=info.zmax, has_latch=bool(info.has_latch), latch=latch,
-               new_history=newh.astype(bool))
-    return parts, out
+def _rot(axis, c, s):
+    # egs++ EGS_RotationMatrix::rotX/rotY/rotZ (egs++/egs_transformations.h:303-326)
+    if axis == 0:
+        return [[1.0, 0.0, 0.0], [0.0, c, s], [0.0, -s, c]]
+    if axis == 1:
+        return [[c, 0.0, -s], [0.0, 1.0, 0.0], [s, 0.0, c]]
+    return [[c, s, 0.0], [-s, c, 0.0], [0.0, 0.0, 1.0]]
+
+
+def _angle(axis, phi):
+    return _rot(axis, math.cos(phi), math.sin(phi))
+
+
+def _rot_from_vector(v):
+    # the matrix EGS_RotationMatrix(const EGS_Vector &) builds (egs_transformations.h:153-182):
+    # rotY(cos t, -sin t) rotZ(cos p, sin p) with t, p the polar and azimuthal angles of v
+    x, y, z = (float(t) for t in v)
+    sinz = x * x + y * y
+    norm = sinz + z * z
+    if norm < 1e-10:
+        raise ValueError("no rotation from a zero vector")
+    norm = math.sqrt(norm)
+    if sinz > 1e-10:
+        sinz = math.sqrt(sinz)
+        return _mul(_rot(1, z / norm, -sinz / norm), _rot(2, x / sinz, y / sinz))
+    if z < 0:
+        return _angle(0, math.pi)
+    return _rot(2, 1.0, 0.0)
+
+
+def egs_rotation(rotation=None, rotation_vector=None):
+    """The rotation matrix of an egs++ transformation block
+    (EGS_AffineTransform::getTransformation, egs++/egs_transformations.cpp:44-108):
+    'rotation vector' = v (3 numbers) is the matrix EGS_RotationMatrix(v) builds,
+    rotY(cos t, -sin t) rotZ(cos p, sin p) for the polar and azimuthal angles t,
+    p of v; 'rotation' = phi theta (2 numbers) is R_z(phi) R_x(theta), alpha
+    beta gamma (3 numbers) R_x(alpha) R_y(beta) R_z(gamma), vx vy vz phi (4
+    numbers) R1^T R_z(phi) R1 with R1 the matrix of v, or the 9 matrix elements
+    row by row.  rotX/Y/Z(c, s) are the matrices of egs_transformations.h:303-326;
+    angles in radians.  Formed in the order of operations egs_gpu_app uses, so
+    both give the same bits."""
+    if rotation_vector is not None and len(rotation_vector) == 3:
+        return np.array(_rot_from_vector(rotation_vector))
+    r = [] if rotation is None else [float(t) for t in rotation]
+    if len(r) == 2:
+        m = _mul(_angle(2, r[0]), _angle(0, r[1]))
+    elif len(r) == 3:
+        m = _mul(_mul(_angle(0, r[0]), _angle(1, r[1])), _angle(2, r[2]))
+    elif len(r) == 4:
+        r1 = _rot_from_vector(r[:3])
+        r1t = [[r1[j][i] for j in range(3)] for i in range(3)]
+        m = _mul(_mul(r1t, _angle(2, r[3])), r1)
+    elif len(r) == 9:
+        m = [r[0:3], r[3:6], r[6:9]]
+    else:
+        m = _rot(2, 1.0, 0.0)
+    return np.array(m, dtype=np.float64)
 
 
 def default_config(**kw):

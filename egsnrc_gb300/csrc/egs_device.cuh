@@ -83,6 +83,8 @@ struct Source {
     long long nphsp;      // shape 2: phase-space particles (device, 7 floats each)
     const float *phsp;
     int recycle;
+    int has_rot;          // shape 2: rotate the particles by rot (row-major)
+    double rot[9];
 };
 
 // -------------------------------------------------------------- queues ----

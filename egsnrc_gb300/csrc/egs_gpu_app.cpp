@@ -145,6 +145,71 @@ static bool load_phsp_source(const Item *s, bool iaea, std::vector<float> &phsp,
     return true;
 }
 
+// The rotation of an egs++ transformation block
+// (EGS_AffineTransform::getTransformation, egs++/egs_transformations.cpp:44-108,
+// matrices egs++/egs_transformations.h:153-200, 303-355), row-major into R:
+// 'rotation vector' = v is the matrix EGS_RotationMatrix(v) builds, rotY(cos t,
+// -sin t) rotZ(cos p, sin p) for the polar and azimuthal angles t, p of v;
+// 'rotation' = phi theta is R_z(phi) R_x(theta), alpha beta gamma is
+// R_x(alpha) R_y(beta) R_z(gamma), vx vy vz phi is R1^T R_z(phi) R1 with R1 the
+// matrix of v, nine numbers the matrix itself.  Returns false when the block
+// has no rotation.
+namespace {
+struct M3 {
+    double a[9];
+    M3 operator*(const M3 &o) const {
+        M3 r;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+                r.a[3 * i + j] = a[3 * i] * o.a[j] + a[3 * i + 1] * o.a[3 + j] + a[3 * i + 2] * o.a[6 + j];
+        return r;
+    }
+    M3 t() const { return {{a[0], a[3], a[6], a[1], a[4], a[7], a[2], a[5], a[8]}}; }
+};
+M3 m_eye() { return {{1, 0, 0, 0, 1, 0, 0, 0, 1}}; }
+M3 m_rx(double c, double s) { return {{1, 0, 0, 0, c, s, 0, -s, c}}; }
+M3 m_ry(double c, double s) { return {{c, 0, -s, 0, 1, 0, s, 0, c}}; }
+M3 m_rz(double c, double s) { return {{c, s, 0, -s, c, 0, 0, 0, 1}}; }
+bool m_of_vector(double x, double y, double z, M3 &r) {
+    double sinz = x * x + y * y, norm = sinz + z * z;
+    if (norm < 1e-10) return false;
+    norm = std::sqrt(norm);
+    if (sinz > 1e-10) {
+        sinz = std::sqrt(sinz);
+        r = m_ry(z / norm, -sinz / norm) * m_rz(x / sinz, y / sinz);
+    } else if (z < 0) {
+        r = m_rx(std::cos(M_PI), std::sin(M_PI));
+    } else {
+        r = m_eye();
+    }
+    return true;
+}
+}  // namespace
+
+static bool egs_rotation(const Item *t, double *R) {
+    M3 m = m_eye();
+    auto v = Item::numbers(t->get("rotation vector", ""));
+    auto r = Item::numbers(t->get("rotation", ""));
+    if (v.size() == 3) {
+        if (!m_of_vector(v[0], v[1], v[2], m)) m = m_eye();
+    } else if (r.size() == 2) {
+        m = m_rz(std::cos(r[0]), std::sin(r[0])) * m_rx(std::cos(r[1]), std::sin(r[1]));
+    } else if (r.size() == 3) {
+        m = m_rx(std::cos(r[0]), std::sin(r[0])) * m_ry(std::cos(r[1]), std::sin(r[1])) *
+            m_rz(std::cos(r[2]), std::sin(r[2]));
+    } else if (r.size() == 4) {
+        M3 r1;
+        if (!m_of_vector(r[0], r[1], r[2], r1)) r1 = m_eye();
+        m = r1.t() * m_rz(std::cos(r[3]), std::sin(r[3])) * r1;
+    } else if (r.size() == 9) {
+        for (int k = 0; k < 9; ++k) m.a[k] = r[k];
+    } else {
+        return false;
+    }
+    for (int k = 0; k < 9; ++k) R[k] = m.a[k];
+    return true;
+}
+
 static const char *MEDCH = "123456789ABCDEFGHIJKLMNOPQRSTUVWXYZabcdefghijklmnopqrstuvwxyz";
 
 static bool read_egsphant(const std::string &path, Phantom &P, std::string &err) {
@@ -319,15 +384,17 @@ int main(int argc, char **argv) {
     if (!s) return fail("simulation source '" + sname + "' not defined");
     egsgpu_source src;
     std::memset(&src, 0, sizeof(src));
-    // EGS_TransformedSource (egs++/sources/egs_transformed_source) with a
-    // translation: the inner source's particles are shifted
-    double shift[3] = {0, 0, 0};
+    // EGS_TransformedSource (egs++/sources/egs_transformed_source): the inner
+    // source's particles are rotated by R and shifted by the translation
+    double shift[3] = {0, 0, 0}, rot[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    bool rotated = false;
     if (egsin::norm(s->get("library")) == "egs_transformed_source") {
         const Item *t = s->block("transformation");
         if (t) {
-            if (t->has("rotation") || t->has("rotation vector")) return fail("rotated sources are not supported");
             auto v = Item::numbers(t->get("translation", "0 0 0"));
-            for (int k = 0; k < 3 && k < (int)v.size(); ++k) shift[k] = v[k];
+            if (v.size() == 3)
+                for (int k = 0; k < 3; ++k) shift[k] = v[k];
+            rotated = egs_rotation(t, rot);
         }
         std::string inner = s->get("source name");
         const Item *in = nullptr;
@@ -345,11 +412,15 @@ int main(int argc, char **argv) {
         src.shape = 2;
         src.nphsp = (long long)(phsp.size() / 7);
         src.phsp = phsp.data();
-        for (int k = 0; k < 3; ++k) src.pos[k] = shift[k];
-        src.pos[2] += zplane;
+        // the file's plane z0: R (x, y, z0) + t = R (x, y, 0) + (t + z0 R e_z)
+        for (int k = 0; k < 3; ++k) src.pos[k] = shift[k] + zplane * rot[3 * k + 2];
         src.dir[2] = 1;
+        if (rotated)
+            for (int k = 0; k < 9; ++k) src.rot[k] = rot[k];
     } else if (lib != "egs_parallel_beam")
         return fail("only egs_parallel_beam, egs_phsp_source and iaea_phsp_source sources are supported");
+    if (rotated && lib != "egs_phsp_source" && lib != "iaea_phsp_source")
+        return fail("rotated sources are supported for phase-space sources only");
     if (lib == "egs_parallel_beam") {
     src.charge = (int)s->num("charge", 0);
     auto dir = Item::numbers(s->get("direction", "0 0 1"));

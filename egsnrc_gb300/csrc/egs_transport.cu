@@ -568,6 +568,15 @@ __global__ void k_source(Params<Real> P, Source S0, long long first, long long n
         w = a < 1 ? sqrt(1 - a) : 0.0;
         if (q[6] < 0) w = -w;
         p.wt = (Real)(fabs((double)q[6]) / (S.recycle + 1));
+        if (S.has_rot) {   // EGS_TransformedSource: x' = R (x, y, 0) + t, u' = R u
+            const double *R = S.rot, px = q[2], py = q[3], u0 = u, v0 = v, w0 = w;
+            x = S.pos[0] + (R[0] * px + R[1] * py);
+            y = S.pos[1] + (R[3] * px + R[4] * py);
+            z = S.pos[2] + (R[6] * px + R[7] * py);
+            u = R[0] * u0 + R[1] * v0 + R[2] * w0;
+            v = R[3] * u0 + R[4] * v0 + R[5] * w0;
+            w = R[6] * u0 + R[7] * v0 + R[8] * w0;
+        }
     } else if (S.spectrum == 0) ek = S.energy;
     else {
         double aj = (double)urand<Real>(p.rng) * S.nbins;
@@ -2672,6 +2681,20 @@ static int build_source(const egsgpu_source *s, Source &S, std::vector<double> &
         err = "unsupported source";
         return EGSGPU_ERR_ARG;
     }
+    bool has_rot = false;
+    for (double r : s->rot) has_rot |= r != 0;
+    if (has_rot && s->shape != 2) { err = "a source rotation is supported for phase-space sources only"; return EGSGPU_ERR_ARG; }
+    if (has_rot) {   // R R^T = 1 and det R = +1 to 1e-6
+        const double *R = s->rot;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                double d = R[3 * i] * R[3 * j] + R[3 * i + 1] * R[3 * j + 1] + R[3 * i + 2] * R[3 * j + 2];
+                if (!(std::fabs(d - (i == j)) < 1e-6)) { err = "the source rotation is not a rotation"; return EGSGPU_ERR_ARG; }
+            }
+        double det = R[0] * (R[4] * R[8] - R[5] * R[7]) - R[1] * (R[3] * R[8] - R[5] * R[6]) +
+                     R[2] * (R[3] * R[7] - R[4] * R[6]);
+        if (!(std::fabs(det - 1) < 1e-6)) { err = "the source rotation is not a rotation"; return EGSGPU_ERR_ARG; }
+    }
     if (s->shape == 2) {   // phase-space particles: checked here, copied by the caller
         if (s->nphsp < 1 || !s->phsp || s->recycle < 0) { err = "bad phase-space source"; return EGSGPU_ERR_ARG; }
         S = Source{};
@@ -2680,6 +2703,8 @@ static int build_source(const egsgpu_source *s, Source &S, std::vector<double> &
         S.dir[2] = 1;
         S.nphsp = s->nphsp;
         S.recycle = s->recycle;
+        S.has_rot = has_rot;
+        for (int k = 0; k < 9; ++k) S.rot[k] = s->rot[k];
         double emax = 0;
         for (long long i = 0; i < s->nphsp; ++i) {
             const float *q = s->phsp + 7 * i;

@@ -99,6 +99,13 @@ typedef struct {
     long long nphsp;
     const float *phsp;
     int recycle;
+    /* shape 2: a rotation R (row-major) applied to every particle before pos
+     * is added, as egs++ EGS_TransformedSource applies its affine transform
+     * (egs++/sources/egs_transformed_source, egs++/egs_transformations.h:
+     * 480-540): the particle at (x, y, 0) with direction (u, v, w) starts at
+     * R (x, y, 0) + pos with direction R (u, v, w).  All nine zero: no
+     * rotation.  Must be zero for shapes 0 and 1. */
+    double rot[9];
 } egsgpu_source;
 
 /* Default configuration (the egs_set_defaults profile, FP32 transport). */

@@ -145,6 +145,7 @@ struct Source {
     std::vector<double> wi;
     std::vector<int> bin;
     std::vector<float> phsp;           // phase-space particles (7 floats each)
+    bool has_rot = false;              // phase-space particles rotated by s.rot
 };
 
 struct Tally {
@@ -1568,6 +1569,18 @@ bool source_particle(Run &R, uint32_t hist, Particle &p) {
         w = a < 1 ? std::sqrt(1 - a) : 0.0;
         if (q[6] < 0) w = -w;
         p.wt = std::fabs((double)q[6]) / (S.s.recycle + 1);
+        if (S.has_rot) {
+            // EGS_TransformedSource (egs++/sources/egs_transformed_source) with
+            // EGS_AffineTransform (egs++/egs_transformations.h:480-540):
+            // position R (x, y, 0) + t, direction R u
+            const double *Rm = S.s.rot, px = q[2], py = q[3], u0 = u, v0 = v, w0 = w;
+            x = S.s.pos[0] + (Rm[0] * px + Rm[1] * py);
+            y = S.s.pos[1] + (Rm[3] * px + Rm[4] * py);
+            z = S.s.pos[2] + (Rm[6] * px + Rm[7] * py);
+            u = Rm[0] * u0 + Rm[1] * v0 + Rm[2] * w0;
+            v = Rm[3] * u0 + Rm[4] * v0 + Rm[5] * w0;
+            w = Rm[6] * u0 + Rm[7] * v0 + Rm[8] * w0;
+        }
     } else if (S.s.spectrum == 0) ek = S.s.energy;
     else {
         int np = S.s.nbins;
@@ -1703,6 +1716,9 @@ int oracle_set_source(oracle_handle *h, const egsgpu_source *s) {
     h->O.S.s = *s;
     double n = std::sqrt(s->dir[0] * s->dir[0] + s->dir[1] * s->dir[1] + s->dir[2] * s->dir[2]);
     for (int k = 0; k < 3; ++k) h->O.S.s.dir[k] = s->dir[k] / n;
+    h->O.S.has_rot = false;
+    for (double r : s->rot) h->O.S.has_rot |= r != 0;
+    if (h->O.S.has_rot && s->shape != 2) return 1;
     if (s->shape == 2) {
         if (s->nphsp < 1 || !s->phsp || s->recycle < 0) return 1;
         h->O.S.phsp.assign(s->phsp, s->phsp + 7 * s->nphsp);

@@ -229,6 +229,22 @@ def test_app_latch_filter_matches_binding(tmp_path):
     compare(dose_file, binding_dose(q))
 
 
+def test_app_rotated_phase_space_source_matches_binding(tmp_path):
+    """egs_transformed_source with 'rotation = 1.1 -0.4 0.3' and a translation:
+    the driver builds R_x R_y R_z as egsnrc_gb300.egs_rotation does, so the run
+    equals the binding's with that matrix."""
+    path, p, _ = ex16_particles(tmp_path)
+    text = PHSP.replace("PHSPFILE", str(path)).replace(
+        "translation = 0 0 -0.5", "translation = -1 -20 4\n            rotation = 1.1 -0.4 0.3")
+    dose_file, _ = run_app(tmp_path, text, "phsp_rot")
+    b = -15 + 2.0 * np.arange(16)
+    eng = eg.DoseEngine([W.WATER], ecut=0.7, pcut=0.01)
+    eng.set_geometry(eg.XYZGeometry(b, b, 2.0 * np.arange(16), 0))
+    eng.set_source(eg.PhaseSpaceSource(p, position=(-1, -20, 4), recycle=1, rotation=eg.egs_rotation([1.1, -0.4, 0.3])))
+    eng.run(30000, nbatch=3, seed=3)
+    compare(dose_file, eng.dose()[0])
+
+
 def test_app_presta1_and_smax_match_binding(tmp_path):
     """The transport keys "Boundary crossing algorithm = PRESTA-I", "Skin
     depth for BCA" and "Global Smax" reach the engine as the binding sets them."""

@@ -271,6 +271,37 @@ def egs_rotation(rotation=None, rotation_vector=None):
     return np.array(m, dtype=np.float64)
 
 
+PHSP_FORMATS = {0: "MODE0", 1: "MODE2", 2: "IAEA"}
+
+
+def read_phase_space(path, first=0, count=None):
+    """Reads a phase-space file through the library's reader (egsgpu_read_phsp;
+    host only, no GPU): a BEAMnrc .egsphsp file or an IAEA pair
+    <name>.IAEAheader + <name>.IAEAphsp (path = <name>, with or without either
+    extension).  Returns (particles, info): particles an (count, 7) float32
+    array of {charge, kinetic energy, x, y, u, v, weight} as PhaseSpaceSource
+    takes them; info a dict with format, n, photons, incident, ekmax, zmin,
+    zmax, has_latch, latch and new_history (arrays over the records read)."""
+    L = load_library()
+    info = PhspInfo()
+    p = str(path).encode()
+    rc = L.egsgpu_read_phsp(p, 0, 0, C.byref(info), None, None, None)
+    if rc:
+        raise EGSError(rc, L.egsgpu_last_error(None).decode())
+    n = info.n - first if count is None else count
+    parts = np.zeros((max(n, 0), 7), dtype=np.float32)
+    latch = np.zeros(max(n, 0), dtype=np.uint32)
+    newh = np.zeros(max(n, 0), dtype=np.uint8)
+    rc = L.egsgpu_read_phsp(p, first, n, C.byref(info), parts.ctypes.data_as(C.POINTER(C.c_float)),
+                            latch.ctypes.data_as(C.POINTER(C.c_uint32)), newh.ctypes.data_as(C.POINTER(C.c_ubyte)))
+    if rc:
+        raise EGSError(rc, L.egsgpu_last_error(None).decode())
+    out = dict(format=PHSP_FORMATS[info.format], n=info.n, photons=info.photons, incident=info.incident,
+               ekmax=info.ekmax, zmin=info.zmin, zmax=info.zmax, has_latch=bool(info.has_latch), latch=latch,
+               new_history=newh.astype(bool))
+    return parts, out
+
+
 def default_config(**kw):
     cfg = Config()
     load_library().egsgpu_default_config(C.byref(cfg))

@@ -152,8 +152,8 @@ static bool load_phsp_source(const Item *s, bool iaea, std::vector<float> &phsp,
 // -sin t) rotZ(cos p, sin p) for the polar and azimuthal angles t, p of v;
 // 'rotation' = phi theta is R_z(phi) R_x(theta), alpha beta gamma is
 // R_x(alpha) R_y(beta) R_z(gamma), vx vy vz phi is R1^T R_z(phi) R1 with R1 the
-// matrix of v, nine numbers the matrix itself.  Returns false when the block
-// has no rotation.
+// matrix of v, nine numbers the matrix itself.  Returns 1 with R filled, 0 when
+// the block has no rotation, -1 (message in err) for a zero vector.
 namespace {
 struct M3 {
     double a[9];
@@ -186,12 +186,16 @@ bool m_of_vector(double x, double y, double z, M3 &r) {
 }
 }  // namespace
 
-static bool egs_rotation(const Item *t, double *R) {
+static int egs_rotation(const Item *t, double *R, std::string &err) {
+    auto fail_rot = [&](const char *what) {
+        err = std::string("transformation: ") + what;   // egs++ stops with a fatal error here
+        return -1;
+    };
     M3 m = m_eye();
     auto v = Item::numbers(t->get("rotation vector", ""));
     auto r = Item::numbers(t->get("rotation", ""));
     if (v.size() == 3) {
-        if (!m_of_vector(v[0], v[1], v[2], m)) m = m_eye();
+        if (!m_of_vector(v[0], v[1], v[2], m)) return fail_rot("a rotation vector of length 0");
     } else if (r.size() == 2) {
         m = m_rz(std::cos(r[0]), std::sin(r[0])) * m_rx(std::cos(r[1]), std::sin(r[1]));
     } else if (r.size() == 3) {
@@ -199,15 +203,15 @@ static bool egs_rotation(const Item *t, double *R) {
             m_rz(std::cos(r[2]), std::sin(r[2]));
     } else if (r.size() == 4) {
         M3 r1;
-        if (!m_of_vector(r[0], r[1], r[2], r1)) r1 = m_eye();
+        if (!m_of_vector(r[0], r[1], r[2], r1)) return fail_rot("a rotation axis of length 0");
         m = r1.t() * m_rz(std::cos(r[3]), std::sin(r[3])) * r1;
     } else if (r.size() == 9) {
         for (int k = 0; k < 9; ++k) m.a[k] = r[k];
     } else {
-        return false;
+        return 0;
     }
     for (int k = 0; k < 9; ++k) R[k] = m.a[k];
-    return true;
+    return 1;
 }
 
 static const char *MEDCH = "123456789ABCDEFGHIJKLMNOPQRSTUVWXYZabcdefghijklmnopqrstuvwxyz";
@@ -394,7 +398,10 @@ int main(int argc, char **argv) {
             auto v = Item::numbers(t->get("translation", "0 0 0"));
             if (v.size() == 3)
                 for (int k = 0; k < 3; ++k) shift[k] = v[k];
-            rotated = egs_rotation(t, rot);
+            std::string rerr;
+            const int rc = egs_rotation(t, rot, rerr);
+            if (rc < 0) return fail(rerr);
+            rotated = rc > 0;
         }
         std::string inner = s->get("source name");
         const Item *in = nullptr;

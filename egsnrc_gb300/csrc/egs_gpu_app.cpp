@@ -358,26 +358,6 @@ int main(int argc, char **argv) {
         }
     }
 
-    // ---- engine ----
-    egsgpu_handle *h = nullptr;
-    int st = egsgpu_create(&cfg, &h);
-    if (st) return fail("egsgpu_create failed with status " + std::to_string(st));
-    std::vector<const char *> names;
-    for (auto &m : P.media) names.push_back(m.c_str());
-    if ((st = egsgpu_load_media(h, data.c_str(), pegs_file.c_str(), names.data(), (int)names.size())))
-        return fail(egsgpu_last_error(h));
-    if (P.abs_density) {   // relative density = mass density / PEGS4 density
-        P.rhor.resize(P.rho_abs.size());
-        for (size_t i = 0; i < P.rho_abs.size(); ++i) {
-            double info[4];
-            egsgpu_get_medium(h, P.med[i], info);
-            P.rhor[i] = P.rho_abs[i] / info[0];
-        }
-    }
-    if ((st = egsgpu_set_xyz_geometry(h, P.nx, P.ny, P.nz, P.xb.data(), P.yb.data(), P.zb.data(), P.med.data(),
-                                      P.rhor.data())))
-        return fail(egsgpu_last_error(h));
-
     // ---- source (EGS_ParallelBeam; egs_base_source.cpp:46, egs_parallel_beam.cpp:43) ----
     const Item *sd = root->block("source definition");
     if (!sd) return fail("no source definition");
@@ -411,6 +391,7 @@ int main(int argc, char **argv) {
         s = in;
     }
     std::vector<float> phsp;
+    std::vector<double> edges, weights;   // the source points into these until egsgpu_set_source
     std::string lib = egsin::norm(s->get("library"));
     if (lib == "egs_phsp_source" || lib == "iaea_phsp_source") {
         double zplane = 0;
@@ -454,7 +435,6 @@ int main(int argc, char **argv) {
     } else return fail("shape type '" + sh->get("type") + "' is not supported");
     const Item *sp = s->block("spectrum");
     if (!sp) return fail("source has no spectrum");
-    std::vector<double> edges, weights;
     std::string sptype = egsin::norm(sp->get("type"));
     if (sptype == "monoenergetic") {
         src.spectrum = 0;
@@ -473,6 +453,26 @@ int main(int argc, char **argv) {
     for (int k = 0; k < 3; ++k) src.pos[k] += shift[k];
     src.xmin += shift[0]; src.xmax += shift[0]; src.ymin += shift[1]; src.ymax += shift[1];
     }
+    // ---- engine (after the whole input has been read: input errors need no GPU) ----
+    egsgpu_handle *h = nullptr;
+    int st = egsgpu_create(&cfg, &h);
+    if (st) return fail("egsgpu_create failed with status " + std::to_string(st));
+    std::vector<const char *> names;
+    for (auto &m : P.media) names.push_back(m.c_str());
+    if ((st = egsgpu_load_media(h, data.c_str(), pegs_file.c_str(), names.data(), (int)names.size())))
+        return fail(egsgpu_last_error(h));
+    if (P.abs_density) {   // relative density = mass density / PEGS4 density
+        P.rhor.resize(P.rho_abs.size());
+        for (size_t i = 0; i < P.rho_abs.size(); ++i) {
+            double info[4];
+            egsgpu_get_medium(h, P.med[i], info);
+            P.rhor[i] = P.rho_abs[i] / info[0];
+        }
+    }
+    if ((st = egsgpu_set_xyz_geometry(h, P.nx, P.ny, P.nz, P.xb.data(), P.yb.data(), P.zb.data(), P.med.data(),
+                                      P.rhor.data())))
+        return fail(egsgpu_last_error(h));
+
     if ((st = egsgpu_set_source(h, &src))) return fail(egsgpu_last_error(h));
 
     uint32_t seed = 1;

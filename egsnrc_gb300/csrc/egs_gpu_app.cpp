@@ -8,7 +8,10 @@
 // ones egs_app reads (run control, geometry definition, media, source
 // definition, MC transport parameter, rng definition, ausgab object
 // definition), the PEGS4 file is given with -p, and the dose goes to
-// <name>.3ddose in the egs_dose_scoring format.
+// <name>.3ddose in the egs_dose_scoring format, normalised as EGS_DoseScoring
+// normalises it: the dose per history times ncase / F, F the source's fluence
+// (ncase / area for a parallel beam; for a phase-space source the incident
+// particles of the original simulation times the fraction of the file read).
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -73,7 +76,7 @@ static bool planes(const Item *g, const char *p, const char *s, std::vector<doub
 // ('reuse photons/electrons', or 'recycle ...') must be the same number for
 // both.  Returns the plane z of the particles in *zplane.
 static bool load_phsp_source(const Item *s, bool iaea, std::vector<float> &phsp, int &recycle, double &zplane,
-                             std::string &err) {
+                             double &incident, std::string &err) {
     const std::string path = s->get(iaea ? "iaea phase space file" : "phase space file");
     egsgpu_phsp_info info;
     if (egsgpu_read_phsp(path.c_str(), 0, 0, &info, nullptr, nullptr, nullptr)) {
@@ -141,6 +144,7 @@ static bool load_phsp_source(const Item *s, bool iaea, std::vector<float> &phsp,
         if ((filter1 && !(latch[k] & filter1)) || (latch[k] & filter2)) keep = false;
         if (!keep) phsp[i + 6] = phsp[i + 6] < 0 ? -0.0f : 0.0f;
     }
+    incident = info.incident;
     std::printf("phase space: %lld particles, %.0f incident histories\n", info.n, info.incident);
     return true;
 }
@@ -392,11 +396,20 @@ int main(int argc, char **argv) {
     }
     std::vector<float> phsp;
     std::vector<double> edges, weights;   // the source points into these until egsgpu_set_source
+    // EGS_DoseScoring scales the dose per history by ncase / F, F the source's
+    // fluence (egs_dose_scoring.cpp:309-320): ncase / area for EGS_ParallelBeam
+    // (egs_parallel_beam.h:157), so the factor is the shape's area (1 for a point)
+    double norm_e = 1;
     std::string lib = egsin::norm(s->get("library"));
     if (lib == "egs_phsp_source" || lib == "iaea_phsp_source") {
-        double zplane = 0;
+        double zplane = 0, incident = 0;
         std::string perr;
-        if (!load_phsp_source(s, lib == "iaea_phsp_source", phsp, src.recycle, zplane, perr)) return fail(perr);
+        if (!load_phsp_source(s, lib == "iaea_phsp_source", phsp, src.recycle, zplane, incident, perr))
+            return fail(perr);
+        // fluence F = Pinc * Nread / Nparticle (egs_phsp_source.h:153-156): Nread
+        // records are read for ncase histories, each used recycle + 1 times
+        const double nread = (double)((ncase + src.recycle) / (src.recycle + 1));
+        if (incident > 0 && nread > 0) norm_e = (double)ncase / (incident * nread / (double)(phsp.size() / 7));
         src.shape = 2;
         src.nphsp = (long long)(phsp.size() / 7);
         src.phsp = phsp.data();
@@ -431,6 +444,7 @@ int main(int argc, char **argv) {
         src.shape = 1;
         src.xmin = std::min(r[0], r[2]) + tr[0]; src.xmax = std::max(r[0], r[2]) + tr[0];
         src.ymin = std::min(r[1], r[3]) + tr[1]; src.ymax = std::max(r[1], r[3]) + tr[1];
+        norm_e = (src.xmax - src.xmin) * (src.ymax - src.ymin);
         src.pos[2] = tr[2];
     } else return fail("shape type '" + sh->get("type") + "' is not supported");
     const Item *sp = s->block("spectrum");
@@ -492,6 +506,7 @@ int main(int argc, char **argv) {
     egsgpu_get_tallies(h, nullptr, nullptr, tot);
     std::printf("histories %lld in %d batches, %.3f s (%.4g histories/s)\n", ncase, nbatch, dt, ncase / dt);
     std::printf("deposited %.6g MeV, escaped %.6g MeV per history\n", tot[2] / ncase, tot[3] / ncase);
+    std::printf("dose normalisation ncase / fluence = %.6g\n", norm_e);
 
     // .3ddose (egs_dose_scoring.cpp:416-480)
     std::string fn = out + ".3ddose";
@@ -502,7 +517,7 @@ int main(int argc, char **argv) {
         for (double v : *b) std::fprintf(f, "%g ", (float)v);
         std::fprintf(f, "\n");
     }
-    for (size_t i = 0; i < nv; ++i) std::fprintf(f, "%g ", (float)dose[i]);
+    for (size_t i = 0; i < nv; ++i) std::fprintf(f, "%g ", (float)(dose[i] * norm_e));
     std::fprintf(f, "\n");
     for (size_t i = 0; i < nv; ++i) std::fprintf(f, "%g ", (float)(dose[i] > 0 ? sig[i] / dose[i] : 1.0));
     std::fprintf(f, "\n");

@@ -127,6 +127,13 @@ def run_app(tmp_path, text, name):
     return dose, rel
 
 
+def phsp_norm(nparticles, incident, ncase=30000, recycle=1):
+    """EGS_DoseScoring's factor ncase / F for a phase-space source, F = incident
+    * Nread / Nparticle with Nread the records read for ncase histories."""
+    nread = (ncase + recycle) // (recycle + 1)
+    return ncase / (incident * nread / nparticles)
+
+
 def compare(dose_file, dose_py):
     # the file holds %g of the single-precision dose (6 digits); doses are
     # ~1e-11 Gy per history, so the comparison is relative only
@@ -160,7 +167,7 @@ def test_app_phase_space_source_matches_binding(tmp_path):
     eng.set_geometry(g)
     eng.set_source(eg.PhaseSpaceSource(p, position=(0, 0, -0.5), recycle=1))
     eng.run(30000, nbatch=3, seed=3)
-    compare(dose_file, eng.dose()[0])
+    compare(dose_file, eng.dose()[0] * phsp_norm(len(p), 15000))
 
 
 def ex16_particles(tmp_path):
@@ -172,12 +179,13 @@ def ex16_particles(tmp_path):
 
 
 def binding_dose(p, recycle=1):
+    """The binding's dose per history, times the driver's phase-space normalisation."""
     b = -15 + 2.0 * np.arange(16)
     eng = eg.DoseEngine([W.WATER], ecut=0.7, pcut=0.01)
     eng.set_geometry(eg.XYZGeometry(b, b, 2.0 * np.arange(16), 0))
     eng.set_source(eg.PhaseSpaceSource(p, position=(0, 0, -0.5), recycle=recycle))
     eng.run(30000, nbatch=3, seed=3)
-    return eng.dose()[0]
+    return eng.dose()[0] * phsp_norm(len(p), 15000, recycle=recycle)
 
 
 def test_app_iaea_phase_space_source_matches_binding(tmp_path):
@@ -242,7 +250,7 @@ def test_app_rotated_phase_space_source_matches_binding(tmp_path):
     eng.set_geometry(eg.XYZGeometry(b, b, 2.0 * np.arange(16), 0))
     eng.set_source(eg.PhaseSpaceSource(p, position=(-1, -20, 4), recycle=1, rotation=eg.egs_rotation([1.1, -0.4, 0.3])))
     eng.run(30000, nbatch=3, seed=3)
-    compare(dose_file, eng.dose()[0])
+    compare(dose_file, eng.dose()[0] * phsp_norm(len(p), 15000))
 
 
 def test_app_presta1_and_smax_match_binding(tmp_path):

@@ -70,12 +70,24 @@ def build_app(force=False):
     return APP
 
 
+def reference_dir():
+    """The reference checkout used to build oracle/_ref, or None."""
+    for d in (os.environ.get("EGSNRC_REFERENCE"), "/root/reference"):
+        if d and os.path.isdir(os.path.join(d, "HEN_HOUSE")):
+            return d
+    return None
+
+
 def build_oracle(force=False):
     if force and os.path.exists(ORACLE_LIB):
         os.remove(ORACLE_LIB)
     _run(["make", "-s"], cwd=ORACLE_DIR)
-    # the reference's own IAEA phase-space library, where its sources are present
-    _run(["make", "-s", "ref"], cwd=ORACLE_DIR)
+    # the reference's own code that compiles standalone (oracle/_ref), where
+    # its sources are present: EGSNRC_REFERENCE names the checkout (the
+    # directory holding HEN_HOUSE)
+    ref = reference_dir()
+    if ref:
+        _run(["make", "-s", "ref", "REF=" + ref], cwd=ORACLE_DIR)
     return ORACLE_LIB
 
 

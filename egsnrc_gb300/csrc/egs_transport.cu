@@ -116,6 +116,7 @@ constexpr int LSTACK = 6;   // per-thread LIFO depth for charged secondaries
 // loop before the warp's bookkeeping (refill, interaction batching) runs again.
 constexpr int PHOTON_HOPS = 8;
 constexpr int INTER_MAXWAIT = 24;   // longest wait of a lane due to interact
+constexpr int MAX_BLOCK = 128;      // launch bound of the transport kernels (threads per CTA)
 
 // ------------------------------------------------------------- tallies ----
 template <class Real>
@@ -650,7 +651,7 @@ struct PhotonState {
 // (+5% on slab phantoms over the unbounded 94-register build); the FP64 build
 // would spill ~1 KB per thread at that bound and keeps its registers.
 template <class Real, bool Multi, bool Adj = false, bool HFL = false>
-__global__ void __launch_bounds__(128, sizeof(Real) == 4 ? 8 : 1) k_photon(Params<Real> P) {
+__global__ void __launch_bounds__(MAX_BLOCK, sizeof(Real) == 4 ? 8 : 1) k_photon(Params<Real> P) {
     const Tables<Real> &T = P.T;
     const Geom<Real> &G = P.G;
     const unsigned lane = threadIdx.x & 31u;
@@ -940,7 +941,7 @@ __device__ inline Real eloss_g(const Tables<Real> &T, const MedScalars<Real> &M,
 // once at its end by mscat.  Its own instantiation, so that the EXACT kernels
 // carry none of this code.
 template <class Real, bool Multi, bool Adj = false, bool HFL = false, bool PI = false>
-__global__ void __launch_bounds__(128) k_electron(Params<Real> P) {
+__global__ void __launch_bounds__(MAX_BLOCK) k_electron(Params<Real> P) {
     const Tables<Real> &T = P.T;
     const Geom<Real> &G = P.G;
     const unsigned lane = threadIdx.x & 31u;
@@ -2473,11 +2474,14 @@ struct Engine : EngineBase {
             q.capacity = cap;
         }
         if ((size_t)(b - scratch) > scratch_bytes) { err = "no-allocation scratch layout overflow"; return EGSGPU_ERR_STATE; }
-        const int bs = 128;
+        // launch shapes and interaction batching as egsgpu_run takes them
+        const int bs = cfg.block_size > 0 ? cfg.block_size : 128;
         int occ_p = 1, occ_e = 1;
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, false>, bs, 0));
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, false>, bs, 0));
-        const int gp = sm_count * std::max(1, occ_p), ge = sm_count * std::max(1, occ_e);
+        const int cps_cap = cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm : 64;
+        const int gp = sm_count * std::max(1, std::min(cps_cap, occ_p));
+        const int ge = sm_count * std::max(1, std::min(cps_cap, occ_e));
         Params<Real> P;
         std::memset(&P, 0, sizeof(P));
         P.T = T; P.G = G;
@@ -2486,7 +2490,7 @@ struct Engine : EngineBase {
         P.energy = energy; P.counters = counters; P.error = error; P.peak = counts + 8;
         P.seed = seed;
         P.requeue_lanes = 0;
-        P.inter_batch = 12;
+        P.inter_batch = cfg.inter_batch > 0 ? std::min(cfg.inter_batch, 32) : (cfg.inter_batch < 0 ? 1 : 8);
         // the array keeps the previous call's contents: clear the counters
         CK(cudaMemsetAsync(scratch, 0, 1024, st));
         CK(cudaMemsetAsync(dose, 0, (size_t)nvox * sizeof(double), st));
@@ -2593,6 +2597,8 @@ int egsgpu_create(const egsgpu_config *cfg, egsgpu_handle **out) {
     if (!cfg || !out) return EGSGPU_ERR_ARG;
     *out = nullptr;
     if (cfg->precision != 32 && cfg->precision != 64) return EGSGPU_ERR_ARG;
+    // the transport kernels are compiled for at most MAX_BLOCK threads per CTA
+    if (cfg->block_size < 0 || cfg->block_size > MAX_BLOCK || cfg->block_size % 32) return EGSGPU_ERR_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return EGSGPU_ERR_CUDA;
     auto *h = new egsgpu_handle();
@@ -3090,10 +3096,10 @@ int egsgpu_restore(egsgpu_handle *h, const void *buf, size_t size) {
 }  // extern "C"
 
 // Scratch of egsgpu_run_noalloc, the entry point for callers that may not
-// allocate device memory while they transport: code recording a CUDA stream
-// capture (an allocation there is an error or leaves the graph owning the
-// memory), a time-critical loop that must not wait on the allocator, or a host
-// framework whose memory pool owns every allocation on the device.  The array
+// allocate device memory while they transport: a time-critical loop that must
+// not wait on the allocator, or a host framework whose memory pool owns every
+// allocation on the device.  The call still synchronises its stream once per
+// wavefront round to learn whether the queues have drained.  The array
 // is a fixed part of the module: it exists on every GPU the library is used
 // on and costs EGSGPU_NOALLOC_SCRATCH_MIB of device memory there until the
 // process exits.  Host code cannot use the name as an address; the device
@@ -3118,6 +3124,7 @@ int egsgpu_run_noalloc(egsgpu_handle *h, long long first, long long n, uint32_t 
     }
     if (!h->have_media || !h->have_geom || !h->have_source) { h->err = "media, geometry and source must be set"; return EGSGPU_ERR_STATE; }
     if (h->cfg.bca_algorithm != 0) { h->err = "egsgpu_run_noalloc uses EXACT boundary crossing only"; return EGSGPU_ERR_ARG; }
+    if (h->cfg.howfarless > 0) { h->err = "egsgpu_run_noalloc transports voxel by voxel only (no HOWFARLESS)"; return EGSGPU_ERR_ARG; }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) { h->err = "no current CUDA device"; return EGSGPU_ERR_CUDA; }
     unsigned char *scratch = nullptr;

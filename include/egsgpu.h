@@ -241,10 +241,9 @@ int egsgpu_checkpoint(egsgpu_handle *h, void *buf, size_t *size);
 int egsgpu_restore(egsgpu_handle *h, const void *buf, size_t size);
 
 /* No-allocation transport, for callers that may not allocate device memory
- * while they run: code inside a CUDA stream capture, a real-time loop that
- * must not block on the allocator, or a host framework that owns every
- * allocation (its memory pool) and forbids others.  This entry point has no
- * counterpart in the reference API.
+ * while they run: a real-time loop that must not block on the allocator, or a
+ * host framework that owns every allocation (its memory pool) and forbids
+ * others.  This entry point has no counterpart in the reference API.
  *
  * Transports histories [first, first+n) exactly as egsgpu_run would (same
  * random-number streams, same physics) and writes this call's deposited
@@ -257,7 +256,11 @@ int egsgpu_restore(egsgpu_handle *h, const void *buf, size_t size);
  * EGSGPU_NOALLOC_MAX_HISTORIES histories per call (larger n is rejected with
  * EGSGPU_ERR_ARG); a chunk whose secondaries overflow the queues returns
  * EGSGPU_ERR_CAPACITY.  All work is ordered on `stream` (NULL = default
- * stream) and the call returns after it completes.  The first call on each
+ * stream); the call synchronises that stream once per wavefront round, to
+ * learn whether the queues have drained, and returns after the work
+ * completes.  Block size, CTAs per SM and interaction batching are taken
+ * from the handle's configuration as egsgpu_run takes them; the HOWFARLESS
+ * and PRESTA-I options are refused (EGSGPU_ERR_ARG).  The first call on each
  * device looks up the array's device address with cudaGetSymbolAddress;
  * make that first call before any stream capture.  Every call shares the
  * one array: calls that overlap on the GPU (from several threads, streams

@@ -67,3 +67,20 @@ def test_noalloc_rejects_oversized_calls():
     L = eg.load_library()
     assert L.egsgpu_run_noalloc(eng.h, 0, 10, 1, None, None) == 1
     eng.close()
+
+
+@pytest.mark.parametrize("option", [{"howfarless": 1}, {"bca_algorithm": 1}])
+def test_noalloc_refuses_other_transport_modes(option):
+    # HOWFARLESS and PRESTA-I have kernels of their own that the fixed-scratch
+    # path does not launch: the call must refuse rather than transport with
+    # the default physics
+    import torch
+    wl = W.water30(20)
+    eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], precision=64, **option)
+    eng.set_geometry(wl["geometry"])
+    eng.set_source(wl["source"])
+    dose = torch.zeros(wl["geometry"].nvox, dtype=torch.float64, device="cuda")
+    with pytest.raises(eg.EGSError) as ex:
+        eng.run_noalloc(dose.data_ptr(), 10)
+    assert ex.value.code == 1
+    eng.close()

@@ -34,17 +34,21 @@ ALG_BYTES_PER_PUSH = 48       # one secondary record written to a queue
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="slab64")
-    ap.add_argument("--histories", type=float, default=1e7, help="histories per step (one batch)")
+    ap.add_argument("--histories", type=float, default=1e8,
+                    help="histories per step (one batch); the default is the slab64 configuration's 1e8")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-phantoms leg of the default bench")
     ap.add_argument("--precision", type=int, default=32)
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison leg")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--capacity", type=int, default=0, help="particle-queue capacity (0 = engine default)")
     ap.add_argument("--chunk", type=int, default=0, help="histories per wavefront chunk (0 = automatic)")
+    ap.add_argument("--block-size", type=int, default=0, help="threads per CTA of the transport kernels (0 = engine)")
+    ap.add_argument("--ctas-per-sm", type=int, default=0, help="resident CTAs per SM (0 = as many as fit)")
     ap.add_argument("--clock-period", type=float, default=0.2, help="seconds between clock samples")
     ap.add_argument("--clock-mode", default="nvml", choices=["nvml", "process", "off"])
     ap.add_argument("--adjoint", action="store_true",
@@ -214,19 +218,19 @@ def sigma_eff(sum_, sum2, nb, frac=0.5):
     return float(np.sqrt(np.mean(rel * rel))), int(sel.sum())
 
 
-def cpu_sample(wl, seconds, threads, first):
+def cpu_sample(wl, seconds, threads, seed):
     """Times the CPU oracle on a bounded sample of the workload (rank 0, N = 1)."""
     from oracle.oracle_binding import Oracle
-    ora = Oracle(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"])
+    ora = Oracle(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], fast=True)
     ora.set_geometry(wl["geometry"])
     ora.set_source(wl["source"])
     n0 = 400 * threads
     t0 = time.perf_counter()
-    ora.run(n0, nbatch=1, seed=wl["seed"], first=first, threads=threads)
+    ora.run(n0, nbatch=1, seed=seed, first=0, threads=threads)
     dt0 = time.perf_counter() - t0
     n = max(threads, int(n0 * max(seconds - dt0, 0.5) / max(dt0, 1e-3)))
     t1 = time.perf_counter()
-    ora.run(n, nbatch=1, seed=wl["seed"], first=first + n0, threads=threads)
+    ora.run(n, nbatch=1, seed=seed, first=n0, threads=threads)
     dt = time.perf_counter() - t1
     return n, dt
 
@@ -238,7 +242,7 @@ def reference_arm(args, wl, ws, rank, dist):
     K, W = args.steps, args.warmup
     # size one step to about 4 s of host work
     from oracle.oracle_binding import Oracle
-    ora = Oracle(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"])
+    ora = Oracle(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], fast=True)
     ora.set_geometry(wl["geometry"])
     ora.set_source(wl["source"])
     n0 = 200 * threads
@@ -250,7 +254,7 @@ def reference_arm(args, wl, ws, rank, dist):
     for _ in range(W):
         ora.run(per_step, nbatch=1, seed=wl["seed"], first=first, threads=threads)
         first += per_step
-    ora2 = Oracle(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"])
+    ora2 = Oracle(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], fast=True)
     ora2.set_geometry(wl["geometry"])
     ora2.set_source(wl["source"])
     t0 = time.perf_counter()
@@ -269,7 +273,8 @@ def reference_arm(args, wl, ws, rank, dist):
             "dose_efficiency": eff, "sigma_bar_50pct": sig,
             "cpu_baseline": {"value": value, "unit": "histories/s", "cores": threads, "kind": "port",
                              "sample": "%d histories per step x %d steps of %s (FP64 CPU restatement of the "
-                                       "reference transport, one thread per core)" % (per_step, K, wl["name"])},
+                                       "reference transport, -O3 -ffast-math, one thread per core)"
+                                       % (per_step, K, wl["name"])},
             "e2e": {"value": value, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -306,7 +311,7 @@ def batched_oracle(wl, frac, threads, first):
     """CPU oracle over every phantom of the batched workload, `frac` of each
     phantom's step histories; returns (histories, seconds)."""
     from oracle.oracle_binding import Oracle
-    ora = Oracle(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"])
+    ora = Oracle(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], fast=True)
     n, t = 0, 0.0
     for p in wl["problems"]:
         m = max(threads, int(p["histories"] * frac))
@@ -329,18 +334,25 @@ def batched_config(wl, args):
 
 def bench_batched(args, ws, rank, local, dist):
     """Many phantoms per step (one egsgpu_run_phantoms call) against the same
-    phantoms run one after another."""
+    phantoms run one after another; prints the line."""
+    line = batched_measure(args, ws, rank, local, dist, args.steps, args.warmup, args.no_cpu, 0.25)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+
+
+def batched_measure(args, ws, rank, local, dist, K, Wm, no_cpu, fp64_frac):
+    """The batched64 workload: K timed steps, each one egsgpu_run_phantoms
+    call over all 64 phantoms; returns the JSON line (rank 0) or None."""
     from egsnrc_gb300 import workloads as W
     wl = W.batched64(scale=args.scale)
     ps = wl["problems"]
     for p in ps:          # every rank transports its own histories (weak scaling)
         p["seed"] += 7919 * rank
     H = sum(p["histories"] for p in ps)
-    K, Wm = args.steps, args.warmup
     threads = os.cpu_count() or 1
     if args.impl == "reference":
         if rank != 0:
-            return
+            return None
         n0, t0 = batched_oracle(wl, 2e-3, threads, 0)
         frac = 2e-3 * 4.0 / max(t0, 1e-3)          # about 4 s of host work per step
         for _ in range(Wm):
@@ -358,12 +370,11 @@ def bench_batched(args, ws, rank, local, dist):
                                  "sample": "%.2g of every phantom's step histories per step x %d steps (FP64 CPU "
                                            "restatement, one thread per core)" % (frac, K)},
                 "e2e": {"value": value, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line), flush=True)
-        return
+        return line
     import torch
     import egsnrc_gb300 as eg
     torch.cuda.set_device(local)
-    ekw = dict(capacity=args.capacity, chunk=args.chunk)
+    ekw = dict(capacity=args.capacity, chunk=args.chunk, block_size=args.block_size, ctas_per_sm=args.ctas_per_sm)
     eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], precision=args.precision, **ekw)
     eng.set_phantoms(ps)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
@@ -441,7 +452,7 @@ def bench_batched(args, ws, rank, local, dist):
             "roofline": roof, "gpu_launches": int(launches)}
     if rank == 0 and not args.no_fp64:
         # the same phantoms one after another (egsgpu_run per phantom): FP32, and the plain FP64 form
-        for prec, key, frac in ((args.precision, "one_at_a_time", 1.0), (64, "fp64_one_at_a_time", 0.25)):
+        for prec, key, frac in ((args.precision, "one_at_a_time", 1.0), (64, "fp64_one_at_a_time", fp64_frac)):
             e1 = eg.DoseEngine(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], precision=prec, **ekw)
             n1, T1 = 0, 0.0
             rel2 = []
@@ -469,18 +480,65 @@ def bench_batched(args, ws, rank, local, dist):
         if eff:
             line["efficiency_ratio_batched_fp32_over_fp64"] = eff / line["fp64_one_at_a_time"]["dose_efficiency"]
     line["clocks"] = clk.summary()
-    if rank == 0 and ws == 1 and not args.no_cpu:
+    if rank == 0 and ws == 1 and not no_cpu:
         n0, t0 = batched_oracle(wl, 1e-3, threads, 10 ** 8)
         frac = 1e-3 * args.cpu_seconds / max(t0, 1e-3)
         n, dt = batched_oracle(wl, frac, threads, 2 * 10 ** 8)
         line["cpu_baseline"] = {"value": n / dt, "unit": "histories/s", "cores": threads, "kind": "port",
                                 "sample": "%d histories over all %d phantoms on %d host threads, %.1f s"
                                           % (n, len(ps), threads, dt)}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    if dist:
-        dist.barrier()
-        dist.destroy_process_group()
+    return line if rank == 0 else None
+
+
+def fp32_vs_fp64(wl, eg, ekw, n, seed, nb=10):
+    """The FP32 build's error against the FP64 build on the same histories
+    (common random numbers), nb batches of n/nb: relative difference of the
+    total deposited energy with its standard error from the paired batches,
+    and per voxel above 20% of Dmax the paired z = mean difference / its
+    standard error (mean z^2 is 1 for an unbiased FP32 build) and the median
+    relative difference."""
+    per = n // nb
+    out = {}
+    for prec in (32, 64):
+        e = eg.DoseEngine(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], precision=prec, **ekw)
+        e.set_geometry(wl["geometry"])
+        e.set_source(wl["source"])
+        prev = np.zeros(wl["geometry"].nvox)
+        rows = []
+        for b in range(nb):
+            e.run(per, nbatch=1, seed=seed, first=b * per)
+            s, _, _ = e.tallies()
+            rows.append(s - prev)
+            prev = s
+        out[prec] = np.array(rows)
+        wide = e.profile().get("electron_wide_steps", 0.0) if prec == 32 else None
+        steps = e.profile()["electron_steps"] if prec == 32 else None
+        e.close()
+    d = out[32] - out[64]
+    ref = out[64].mean(axis=0)
+    sel = ref > 0.2 * ref.max()
+    md, sd = d.mean(axis=0)[sel], d.std(axis=0, ddof=1)[sel]
+    z = np.where(sd > 0, md / np.maximum(sd / np.sqrt(nb), 1e-300), 0.0)
+    bt = d.sum(axis=1)
+    tot = out[64].sum()
+    return {"histories": int(per * nb), "batches": nb, "total_rel": float(bt.sum() / tot),
+            "total_rel_sigma": float(bt.std(ddof=1) * np.sqrt(nb) / tot), "voxels": int(sel.sum()),
+            "voxel_mean_z2": float(np.mean(z * z)), "voxel_frac_abs_z_lt2": float(np.mean(np.abs(z) < 2)),
+            "voxel_median_rel": float(np.median(np.abs(md) / ref[sel])),
+            "electron_steps_in_fp64": float(wide / steps) if steps else 0.0}
+
+
+def simt_roofline(prof):
+    """Lane occupancy of the transport kernels' persistent warps, from the
+    engine's device counters: mean busy lanes per warp iteration out of 32
+    (the ceiling of SIMT efficiency; divergence within the step lowers the
+    issued fraction further, see the ncu summaries in profiles/)."""
+    out = {}
+    for k in ("photon", "electron"):
+        b = prof.get(k + "_busy_lanes", 0.0)
+        out[k] = {"busy_lanes_per_iteration": b, "frac": b / 32.0,
+                  "steps_per_s": prof[k + "_steps"] / (prof["ms_" + k] / 1e3) if prof["ms_" + k] > 0 else None}
+    return out
 
 
 def adjoint_leg(args, wl, eg, ekw, H):
@@ -516,8 +574,10 @@ def main():
     ws, rank, local, dist = dist_setup(args)
     if args.workload == "batched64":
         bench_batched(args, ws, rank, local, dist)
-        if dist and args.impl == "reference":
+        if dist:
             dist.barrier()
+            if args.impl != "reference":
+                dist.destroy_process_group()
         return
     wl = W.WORKLOADS[args.workload]()
     if args.impl == "reference":
@@ -530,17 +590,23 @@ def main():
     torch.cuda.set_device(local)
     H = int(args.histories)
     K, Wm = args.steps, args.warmup
-    ekw = dict(capacity=args.capacity, chunk=args.chunk, howfarless=int(args.howfarless))
+    ekw = dict(capacity=args.capacity, chunk=args.chunk, howfarless=int(args.howfarless), block_size=args.block_size,
+               ctas_per_sm=args.ctas_per_sm)
     eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], precision=args.precision, **ekw)
     eng.set_geometry(wl["geometry"])
     eng.set_source(wl["source"])
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     flush.zero_()   # loads torch's fill kernel before anything is timed
     torch.cuda.synchronize()
-    base = rank * 2 * (K + Wm + 1) * H     # disjoint history ranges per rank (device-timed and e2e legs)
-    first = base
+    # History indices are 32-bit Philox keys: each leg (device-timed, e2e,
+    # FP64, FP32-vs-FP64, CPU sample) and each rank draws from its own seed
+    # and counts histories from 0, so no leg repeats another's histories.
+    seed0 = wl["seed"] + 7919 * rank
+    if (K + Wm) * H >= 2 ** 32:
+        raise SystemExit("steps x histories per step must stay below 2^32 histories per leg")
+    first = 0
     for _ in range(Wm):
-        eng.run(H, nbatch=1, seed=wl["seed"], first=first)
+        eng.run(H, nbatch=1, seed=seed0, first=first)
         first += H
     eng.reset()
     torch.cuda.synchronize()
@@ -553,7 +619,7 @@ def main():
         start.record()
         for _ in range(K):
             flush.zero_()
-            eng.run(H, nbatch=1, seed=wl["seed"], first=first)
+            eng.run(H, nbatch=1, seed=seed0, first=first)
             first += H
         stop.record()
         torch.cuda.synchronize()
@@ -600,9 +666,11 @@ def main():
 
     host_out = pinned_pair(g.nvox)   # the caller's tally buffers, pinned and reused every step
 
+    first = 0
+
     def e2e_step(first):
         e2e_eng.set_geometry(g)
-        e2e_eng.run(H, nbatch=1, seed=wl["seed"], first=first)
+        e2e_eng.run(H, nbatch=1, seed=seed0 + 1000, first=first)
         return e2e_eng.tallies(out=host_out)
     for _ in range(Wm):   # the same untimed warm-up as the device-timed leg
         e2e_step(first)
@@ -634,31 +702,46 @@ def main():
     if rank == 0 and args.adjoint:
         line["adjoint"] = adjoint_leg(args, wl, eg, ekw, H)
     if rank == 0 and not args.no_fp64 and args.precision == 32:
-        # plain FP64 GPU form on the same problem: histories/s and efficiency
+        # the plain FP64 GPU form on the same problem, timed the same way
+        # (CUDA events on the launching stream around 2 steps of H/10)
         e64 = eg.DoseEngine(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], precision=64, **ekw)
         e64.set_geometry(g)
         e64.set_source(wl["source"])
         H64 = max(H // 10, 100000)
-        e64.run(H64 // 4, nbatch=1, seed=wl["seed"], first=first)
+        first = 0
+        e64.run(H64 // 4, nbatch=1, seed=seed0 + 2000, first=first)
+        first += H64 // 4
         e64.reset()
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(4):
-            e64.run(H64, nbatch=1, seed=wl["seed"], first=first)
+        start.record()
+        for _ in range(2):
+            flush.zero_()
+            e64.run(H64, nbatch=1, seed=seed0 + 2000, first=first)
             first += H64
+        stop.record()
         torch.cuda.synchronize()
-        T64 = time.perf_counter() - t0
+        T64 = start.elapsed_time(stop) / 1e3
         s64, s264, _ = e64.tallies()
-        sig64, _ = sigma_eff(s64, s264, 4)
+        sig64, _ = sigma_eff(s64, s264, 2)
         eff64 = 1.0 / (sig64 * sig64 * T64) if sig64 else None
-        line["fp64"] = {"value": 4 * H64 / T64, "unit": "histories/s", "dose_efficiency": eff64,
-                        "histories_per_step": H64, "steps": 4}
+        e64.close()
+        line["fp64"] = {"value": 2 * H64 / T64, "unit": "histories/s", "dose_efficiency": eff64,
+                        "histories_per_step": H64, "steps": 2, "timing": "CUDA events"}
         if eff and eff64:
             line["efficiency_ratio_fp32_over_fp64"] = eff / eff64
+        line["fp32_vs_fp64"] = fp32_vs_fp64(wl, eg, ekw, max(H // 100, 200000), seed0 + 3000)
+    line["simt"] = simt_roofline(prof)
     line["clocks"] = clk.summary()
+    if rank == 0 and ws == 1 and not args.no_batched and args.workload == "slab64":
+        # the batched configuration (64 phantoms per launch sequence) beside the headline
+        b = batched_measure(args, 1, 0, local, None, 3, 3, True, 0.05)
+        keep = ("value", "unit", "ms_per_step", "config", "dose_efficiency", "sigma_bar_50pct", "e2e",
+                "one_at_a_time", "fp64_one_at_a_time", "efficiency_ratio_batched_fp32_over_fp64", "gpu_launches")
+        line["batched64"] = {k: b[k] for k in keep if k in b}
+        line["batched64"]["steps"] = 3
     if rank == 0 and ws == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        n, dt = cpu_sample(wl, args.cpu_seconds, threads, first + 10 ** 8)
+        n, dt = cpu_sample(wl, args.cpu_seconds, threads, seed0 + 4000)
         line["cpu_baseline"] = {"value": n / dt, "unit": "histories/s", "cores": threads, "kind": "port",
                                 "sample": "%d histories of %s on %d host threads, %.1f s" % (n, wl["name"],
                                                                                           threads, dt)}

@@ -34,7 +34,9 @@ class Config(C.Structure):
                 ("skindepth", C.c_double), ("precision", C.c_int), ("block_size", C.c_int),
                 ("ctas_per_sm", C.c_int), ("chunk", C.c_longlong), ("capacity", C.c_longlong),
                 ("requeue_lanes", C.c_int), ("use_graph", C.c_int), ("inter_batch", C.c_int),
-                ("howfarless", C.c_int), ("smax", C.c_double), ("bca_algorithm", C.c_int)]
+                ("howfarless", C.c_int), ("smax", C.c_double), ("bca_algorithm", C.c_int),
+                ("loop_cap", C.c_int), ("step_cap", C.c_int), ("smem_tables", C.c_int),
+                ("fp64_near_faces", C.c_int)]
 
 
 class SourceStruct(C.Structure):
@@ -88,6 +90,8 @@ def load_library():
     L.egsgpu_get_medium.argtypes = [vp, C.c_int, dp]
     L.egsgpu_set_history_tally.argtypes = [vp, i64, i64]
     L.egsgpu_get_history_tally.argtypes = [vp, dp]
+    L.egsgpu_geometry_query.argtypes = [vp, C.c_int, i64, vp, vp, vp, vp, vp]
+    L.egsgpu_combine_checkpoints.argtypes = [vp, C.c_size_t, vp, C.c_size_t, vp, C.POINTER(C.c_size_t)]
     L.egsgpu_checkpoint.argtypes = [vp, vp, C.POINTER(C.c_size_t)]
     L.egsgpu_restore.argtypes = [vp, vp, C.c_size_t]
     L.egsgpu_read_phsp.argtypes = [C.c_char_p, i64, i64, C.POINTER(PhspInfo), C.POINTER(C.c_float),
@@ -302,6 +306,33 @@ def read_phase_space(path, first=0, count=None):
     return parts, out
 
 
+def combine_checkpoints(a, b):
+    """The checkpoint of the union of two shards' runs (egsgpu_combine_checkpoints);
+    host only."""
+    L = load_library()
+    n = C.c_size_t(0)
+    rc = L.egsgpu_combine_checkpoints(a, len(a), b, len(b), None, C.byref(n))
+    if rc:
+        raise EGSError(rc, "checkpoints of different phantoms or malformed")
+    out = C.create_string_buffer(n.value)
+    rc = L.egsgpu_combine_checkpoints(a, len(a), b, len(b), out, C.byref(n))
+    if rc:
+        raise EGSError(rc, "shards with different histories per batch")
+    return out.raw
+
+
+def checkpoint_arrays(blob):
+    """Header, energy totals, counters and per-voxel sums of a checkpoint:
+    dict(histories, batches, deposited, escaped, counters[8], sum, sum2)."""
+    hdr = np.frombuffer(blob, dtype=np.int64, count=4)
+    nv = int(hdr[1])
+    en = np.frombuffer(blob, dtype=np.float64, count=2, offset=32)
+    cnt = np.frombuffer(blob, dtype=np.uint64, count=8, offset=48)
+    sums = np.frombuffer(blob, dtype=np.float64, count=2 * nv, offset=112)
+    return dict(histories=int(hdr[2]), batches=int(hdr[3]), deposited=float(en[0]), escaped=float(en[1]),
+                counters=cnt.copy(), sum=sums[:nv].copy(), sum2=sums[nv:].copy())
+
+
 def default_config(**kw):
     cfg = Config()
     load_library().egsgpu_default_config(C.byref(cfg))
@@ -439,14 +470,14 @@ class DoseEngine:
         return d, s
 
     def profile(self):
-        o = np.zeros(18)
+        o = np.zeros(20)
         self._check(self.L.egsgpu_get_profile(self.h, _dp(o)))
         keys = ("source", "photon", "electron", "batch")
         d = {"ms_" + k: o[i] for i, k in enumerate(keys)}
         d.update({"launches_" + k: int(o[4 + i]) for i, k in enumerate(keys)})
         d.update(photon_steps=o[8], electron_steps=o[9], photon_pushes=o[10], electron_pushes=o[11],
                  photon_interactions=o[12], electron_interactions=o[13], chunk=int(o[14]),
-                 graph=bool(o[15]), photon_busy_lanes=o[16], electron_busy_lanes=o[17])
+                 graph=bool(o[15]), photon_busy_lanes=o[16], electron_busy_lanes=o[17], electron_wide_steps=o[18])
         return d
 
     def set_history_tally(self, first, n):
@@ -457,6 +488,21 @@ class DoseEngine:
         out = np.zeros(self._hist_n)
         self._check(self.L.egsgpu_get_history_tally(self.h, _dp(out)))
         return out
+
+    def geometry_query(self, op, ireg=None, x=None, u=None, t=None):
+        """The kernels' geometry functions on the current phantom
+        (egsgpu_geometry_query): op 0 isWhere of x, op 1 howfar from region
+        ireg (howfarFromOut where ireg < 0) along u within t, op 2 hownear.
+        Returns (new regions, distances)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        n = len(x)
+        ireg = np.ascontiguousarray(ireg if ireg is not None else np.zeros(n), dtype=np.int32)
+        u = np.ascontiguousarray(u if u is not None else np.zeros((n, 3)), dtype=np.float64)
+        t = np.array(t if t is not None else np.zeros(n), dtype=np.float64)
+        inew = np.zeros(n, dtype=np.int32)
+        self._check(self.L.egsgpu_geometry_query(self.h, int(op), n, ireg.ctypes.data, x.ctypes.data, u.ctypes.data,
+                                                 t.ctypes.data, inew.ctypes.data))
+        return inew, t
 
     def checkpoint(self):
         size = C.c_size_t(0)

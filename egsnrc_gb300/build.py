@@ -79,9 +79,11 @@ def reference_dir():
 
 
 def build_oracle(force=False):
-    if force and os.path.exists(ORACLE_LIB):
-        os.remove(ORACLE_LIB)
-    _run(["make", "-s"], cwd=ORACLE_DIR)
+    if force:
+        for f in (ORACLE_LIB, os.path.join(ORACLE_DIR, "liboracle_fast.so")):
+            if os.path.exists(f):
+                os.remove(f)
+    _run(["make", "-s", "-j2", "all"], cwd=ORACLE_DIR)
     # the reference's own code that compiles standalone (oracle/_ref), where
     # its sources are present: EGSNRC_REFERENCE names the checkout (the
     # directory holding HEN_HOUSE)

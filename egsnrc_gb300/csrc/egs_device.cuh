@@ -15,7 +15,22 @@ constexpr int NRAY = 100;
 constexpr int MS_NL = 64, MS_NQ = 8, MS_NU = 32;
 constexpr int MAXMED = 16;            // media per problem (constant-memory scalars)
 constexpr int MAXNE = 12;             // elements per medium
-constexpr int LOOP_CAP = 100000;      // cap on every rejection loop
+constexpr int LOOP_CAP_DEFAULT = 100000;   // iterations of one rejection loop
+constexpr int STEP_CAP_DEFAULT = 1 << 22;  // transport steps of one particle
+
+// The caps are set from egsgpu_config before every run (egsgpu_config.loop_cap,
+// .step_cap); a loop or particle that reaches one is abandoned and the run
+// returns EGSGPU_ERR_LOOP.  Each translation unit (FP32, FP64 engine) has its
+// own copy, in its namespace EGSGPU_TU.
+#ifndef EGSGPU_TU
+#define EGSGPU_TU tu32
+#endif
+namespace EGSGPU_TU {
+__constant__ int c_loop_cap = LOOP_CAP_DEFAULT;
+__constant__ int c_step_cap = STEP_CAP_DEFAULT;
+}  // namespace EGSGPU_TU
+#define LOOP_CAP (::egsgpu::EGSGPU_TU::c_loop_cap)
+#define STEP_CAP (::egsgpu::EGSGPU_TU::c_step_cap)
 
 // ------------------------------------------------------------- tables ----
 // Per-medium scalars, one struct per medium in constant memory.

@@ -36,12 +36,6 @@
 #include <vector>
 
 #include "../../include/egsgpu.h"
-#include "egs_device.cuh"
-#include "egs_hatch.h"
-#include "egs_physics.cuh"
-
-namespace cg = cooperative_groups;
-
 // This file is compiled twice: as itself (the FP32 engine and the C ABI) and,
 // through egs_transport_f64.cu, as the FP64 engine without fused multiply-adds.
 // Each compilation keeps its kernels, device constants and engine in its own
@@ -49,6 +43,11 @@ namespace cg = cooperative_groups;
 #ifndef EGSGPU_TU
 #define EGSGPU_TU tu32
 #endif
+#include "egs_device.cuh"
+#include "egs_hatch.h"
+#include "egs_physics.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace egsgpu {
 
@@ -66,13 +65,12 @@ template <class Real> __device__ inline const MedScalars<Real> &cmed(int m);
 template <> __device__ inline const MedScalars<float> &cmed<float>(int m) { return c_med_f[m]; }
 template <> __device__ inline const MedScalars<double> &cmed<double>(int m) { return c_med_d[m]; }
 
-// Counters: 0 photon steps, 1 electron steps, 2 pushes, 3 interactions
-// A particle that needs more iterations than this is retired and reported
-// (EGSGPU_ERR_LOOP); no physical history comes near it.
-constexpr int STEP_CAP = 1 << 22;
+// Counters: 0 photon steps, 1 electron steps, 2 pushes, 3 interactions.
+// A particle that needs more than STEP_CAP steps is retired and reported
+// (EGSGPU_ERR_LOOP); no physical history comes near the default.
 
 enum { CNT_PSTEP = 0, CNT_ESTEP = 1, CNT_PUSH = 2, CNT_INTER = 3, CNT_EPUSH = 4, CNT_EINTER = 5,
-       CNT_PLANES = 6, CNT_PITER = 7, CNT_ELANES = 8, CNT_EITER = 9, CNT_N = 12 };
+       CNT_PLANES = 6, CNT_PITER = 7, CNT_ELANES = 8, CNT_EITER = 9, CNT_EWIDE = 10, CNT_N = 12 };
 
 template <class Real>
 struct Params {
@@ -105,6 +103,8 @@ struct Params {
     uint32_t seed;
     int requeue_lanes;                    // park survivors of warps this sparse (0 = never)
     int inter_batch;                      // lanes due to interact before the warp samples them
+    int esm_rows;                         // electron PWLF rows staged in shared memory (0 = none)
+    int split;                            // FP32 kernels: FP64 near voxel faces and range ends
 };
 
 // A warp whose queue is exhausted parks its particles in the next queue once
@@ -117,6 +117,12 @@ constexpr int LSTACK = 6;   // per-thread LIFO depth for charged secondaries
 constexpr int PHOTON_HOPS = 8;
 constexpr int INTER_MAXWAIT = 24;   // longest wait of a lane due to interact
 constexpr int MAX_BLOCK = 128;      // launch bound of the transport kernels (threads per CTA)
+constexpr double VERY_FAR = 1e30;   // egs++ veryFar (egs++/egs_functions.h:105)
+constexpr int SMEM_TABLES_MAX = 96 * 1024;   // largest electron-table staging per CTA (bytes)
+// Distance to a voxel face (cm) within which an FP32 electron step is computed
+// in FP64 when the precision split is on: 2^-12 cm, about 250 FP32 units in
+// the last place of a coordinate of 16 cm.
+constexpr double NEAR_FACE = 1.0 / 4096.0;
 
 // ------------------------------------------------------------- tallies ----
 template <class Real>
@@ -374,15 +380,54 @@ __device__ inline Real hownear(const Geom<Real> &G, int ireg, Real x, Real y, Re
     t = dmin(t, dmin(z - G.zb[iz], G.zb[iz + 1] - z));
     return t;
 }
+// EGS_PlanesT::isWhere with EGS_BaseGeometry::findRegion (egs++/geometry/
+// egs_planes/egs_planes.h:301-311, egs++/egs_base_geometry.h:178-190): the
+// slab of b[0..n] holding x, -1 outside; a point on an interior plane belongs
+// to the slab below it.
 template <class Real>
 __device__ inline int plane_where(const Real *b, int n, Real x) {
     if (x < b[0] || x > b[n]) return -1;
     int lo = 0, hi = n;
     while (hi - lo > 1) {
         int mid = (lo + hi) >> 1;
-        if (x < b[mid]) hi = mid; else lo = mid;
+        if (x <= b[mid]) hi = mid; else lo = mid;
     }
-    return lo;
+    return hi - 1;
+}
+// EGS_XYZGeometry::howfarFromOut (egs_nd_geometry.h:1281-1379): the region a
+// particle outside the phantom at `pos` enters along `dir` within t (the
+// x faces are tried first, then y, then z), or -1; t receives the distance.
+// Positions are FP64 in both builds, as in the source kernel.
+template <class Real>
+__device__ inline int howfar_from_out(const Geom<Real> &G, const double pos[3], const double dir[3], double &t) {
+    const Real *pl[3] = {G.xb, G.yb, G.zb};
+    const int nn[3] = {G.nx, G.ny, G.nz};
+    for (int a = 0; a < 3; ++a) {
+        int i = -1;
+        double t1 = 0;
+        const double b0 = (double)pl[a][0], bn = (double)pl[a][nn[a]];
+        if (pos[a] <= b0 && dir[a] > 0) { t1 = (b0 - pos[a]) / dir[a]; i = 0; }
+        else if (pos[a] >= bn && dir[a] < 0) { t1 = (bn - pos[a]) / dir[a]; i = nn[a] - 1; }
+        if (i < 0 || !(t1 <= t)) continue;
+        const double q[3] = {pos[0] + dir[0] * t1, pos[1] + dir[1] * t1, pos[2] + dir[2] * t1};
+        int idx[3];
+        bool ok = true;
+        for (int c = 0; c < 3 && ok; ++c) {
+            if (c == a) idx[c] = i;
+            else { idx[c] = plane_where(pl[c], nn[c], (Real)q[c]); ok = idx[c] >= 0; }
+        }
+        if (!ok) continue;
+        const int inew = G.voff + idx[0] + idx[1] * G.nx + idx[2] * G.nxy;
+        if (t1 < (double)G.bt) {   // entering at an edge: the step may end at once
+            Real tt = (Real)t1;
+            int itest = howfar(G, inew, (Real)q[0], (Real)q[1], (Real)q[2], (Real)dir[0], (Real)dir[1], (Real)dir[2], tt);
+            if (itest == -1 && tt < G.bt) return -1;
+            t1 = (double)tt;
+        }
+        t = t1;
+        return inew;
+    }
+    return -1;
 }
 
 
@@ -589,37 +634,15 @@ __global__ void k_source(Params<Real> P, Source S0, long long first, long long n
     p.iq = charge;
     p.E = (Real)(p.iq == 0 ? ek : ek + RM);
     const Geom<Real> &G = geom_of<Real, Multi>(P, k);
-    // isWhere, then howfarFromOut (egs_nd_geometry.h:1281-1379), in FP64
+    // EGS_Application::simulateSingleShower (egs_application.cpp:938-945):
+    // isWhere, then howfarFromOut with t = veryFar and x += u t, in FP64
     int ix = plane_where(G.xb, G.nx, (Real)x), iy = plane_where(G.yb, G.ny, (Real)y), iz = plane_where(G.zb, G.nz, (Real)z);
     int ir = (ix >= 0 && iy >= 0 && iz >= 0) ? G.voff + ix + iy * G.nx + iz * G.nxy : -1;
     if (ir < 0) {
-        const Real *pl[3] = {G.xb, G.yb, G.zb};
-        int nn[3] = {G.nx, G.ny, G.nz};
-        double pos[3] = {x, y, z}, dir[3] = {u, v, w};
-        for (int a = 0; a < 3 && ir < 0; ++a) {
-            int i = -1;
-            double t1 = 0, b0 = (double)pl[a][0], bn = (double)pl[a][nn[a]];
-            if (pos[a] <= b0 && dir[a] > 0) { t1 = (b0 - pos[a]) / dir[a]; i = 0; }
-            else if (pos[a] >= bn && dir[a] < 0) { t1 = (bn - pos[a]) / dir[a]; i = nn[a] - 1; }
-            if (i < 0 || t1 > 1e10) continue;
-            double q[3] = {pos[0] + dir[0] * t1, pos[1] + dir[1] * t1, pos[2] + dir[2] * t1};
-            int idx[3];
-            bool ok = true;
-            for (int c = 0; c < 3; ++c) {
-                if (c == a) { idx[c] = i; continue; }
-                idx[c] = plane_where(pl[c], nn[c], (Real)q[c]);
-                if (idx[c] < 0) { ok = false; break; }
-            }
-            if (!ok) continue;
-            int inew = G.voff + idx[0] + idx[1] * G.nx + idx[2] * G.nxy;
-            if (t1 < (double)G.bt) {
-                Real tt = (Real)t1;
-                int itest = howfar(G, inew, (Real)q[0], (Real)q[1], (Real)q[2], (Real)u, (Real)v, (Real)w, tt);
-                if (itest == -1 && tt < G.bt) break;
-            }
-            x = q[0]; y = q[1]; z = q[2];
-            ir = inew;
-        }
+        const double pos[3] = {x, y, z}, dir[3] = {u, v, w};
+        double t = VERY_FAR;
+        ir = howfar_from_out(G, pos, dir, t);
+        if (ir >= 0) { x += u * t; y += v * t; z += w * t; }
     }
     if (ir < 0) return;
     p.x = (Real)x; p.y = (Real)y; p.z = (Real)z;
@@ -890,46 +913,122 @@ __device__ inline const Real *rrow(const Tables<Real> &T, const MedScalars<Real>
     return T.erange + ((size_t)M.etab_off + lel - 1) * 4;
 }
 
+// The residual-range and energy-loss macros take their arithmetic type C
+// apart from the table type Real: the FP32 kernels run them in FP64 where a
+// step ends near a voxel face or near the end of the range (see
+// k_electron's `wide` steps), from the same FP32 table rows.
 // $COMPUTE-DRANGE (src/egsnrc.macros:3214-3238)
-template <class Real>
-__device__ inline Real drange(const Tables<Real> &T, const MedScalars<Real> &M, int qel, Real e1, Real e2, int lel,
-                            Real el1, Real el2) {
+template <class C, class Real>
+__device__ inline C drange(const Tables<Real> &T, const MedScalars<Real> &M, int qel, C e1, C e2, int lel, C el1,
+                           C el2) {
     const Real *r = erow(T, M, lel);
-    Real fedep = 1 - e2 / e1;
-    Real elktmp = (Real)0.5 * (el1 + el2 + (Real)0.25 * fedep * fedep * (1 + fedep * (1 + (Real)0.875 * fedep)));
-    Real d0 = qel ? (Real)r[6] : (Real)r[4], d1 = qel ? (Real)r[7] : (Real)r[5];
-    Real dedxmid = 1 / (d1 * elktmp + d0);
-    Real aux = d1 * dedxmid;
+    C fedep = 1 - e2 / e1;
+    C elktmp = (C)0.5 * (el1 + el2 + (C)0.25 * fedep * fedep * (1 + fedep * (1 + (C)0.875 * fedep)));
+    C d0 = qel ? (C)r[6] : (C)r[4], d1 = qel ? (C)r[7] : (C)r[5];
+    C dedxmid = 1 / (d1 * elktmp + d0);
+    C aux = d1 * dedxmid;
     aux = aux * (1 + 2 * aux) * (fedep / (2 - fedep)) * (fedep / (2 - fedep)) / 6;
     return fedep * e1 * dedxmid * (1 + aux);
 }
 // $COMPUTE-ELOSS (:3290-3312)
-template <class Real>
-__device__ inline Real eloss(const Tables<Real> &T, const MedScalars<Real> &M, int qel, Real step, Real eke, Real elke,
-                           int lel, Real rhof) {
+template <class C, class Real>
+__device__ inline C eloss(const Tables<Real> &T, const MedScalars<Real> &M, int qel, C step, C eke, C elke, int lel,
+                          C rhof) {
     const Real *r = erow(T, M, lel);
-    Real d0 = qel ? (Real)r[6] : (Real)r[4], d1 = qel ? (Real)r[7] : (Real)r[5];
-    Real dedxmid = d1 * elke + d0;
-    Real aux = d1 / dedxmid;
-    Real de = dedxmid * step * rhof;
-    Real fedep = de / eke;
-    return de * (1 - (Real)0.5 * fedep * aux * (1 - (Real)0.333333 * fedep * (aux - 1 - (Real)0.25 * fedep * (2 - aux * (4 - aux)))));
+    C d0 = qel ? (C)r[6] : (C)r[4], d1 = qel ? (C)r[7] : (C)r[5];
+    C dedxmid = d1 * elke + d0;
+    C aux = d1 / dedxmid;
+    C de = dedxmid * step * rhof;
+    C fedep = de / eke;
+    return de * (1 - (C)0.5 * fedep * aux * (1 - (C)0.333333 * fedep * (aux - 1 - (C)0.25 * fedep * (2 - aux * (4 - aux)))));
 }
 // $COMPUTE-ELOSS-G (:3315-3351)
-template <class Real>
-__device__ inline Real eloss_g(const Tables<Real> &T, const MedScalars<Real> &M, int qel, Real step, Real eke, Real elke,
-                             int lel, Real range, Real rhof) {
-    Real tuss = range - rrow(T, M, lel)[1 + qel] / rhof;
-    if (tuss >= step) return eloss(T, M, qel, step, eke, elke, lel, rhof);
+template <class C, class Real>
+__device__ inline C eloss_g(const Tables<Real> &T, const MedScalars<Real> &M, int qel, C step, C eke, C elke, int lel,
+                            C range, C rhof) {
+    C tuss = range - (C)rrow(T, M, lel)[1 + qel] / rhof;
+    if (tuss >= step) return eloss<C>(T, M, qel, step, eke, elke, lel, rhof);
     int lt = lel;
     tuss = (range - step) * rhof;
-    if (tuss <= 0) return eke - M.te * (Real)0.99;
-    while (lt > 1 && tuss < rrow(T, M, lt)[1 + qel]) --lt;
+    if (tuss <= 0) return eke - (C)M.te * (C)0.99;
+    while (lt > 1 && tuss < (C)rrow(T, M, lt)[1 + qel]) --lt;
     if (lt > M.meke - 1) lt = M.meke - 1;
-    Real elktmp = (lt + 1 - (Real)M.eke0) / (Real)M.eke1, eketmp = rrow(T, M, lt + 1)[0];
-    tuss = (rrow(T, M, lt + 1)[1 + qel] - tuss) / rhof;
-    Real de = eloss(T, M, qel, tuss, eketmp, elktmp, lt, rhof);
+    C elktmp = (lt + 1 - (C)M.eke0) / (C)M.eke1, eketmp = (C)rrow(T, M, lt + 1)[0];
+    tuss = ((C)rrow(T, M, lt + 1)[1 + qel] - tuss) / rhof;
+    C de = eloss<C>(T, M, qel, tuss, eketmp, elktmp, lt, rhof);
     return de + eke - eketmp;
+}
+
+// EGS_XYZGeometry::hownear in arithmetic type C from the kernel's FP32 or
+// FP64 positions and planes.
+template <class C, class Real>
+__device__ inline C hownear_c(const Geom<Real> &G, int ireg, Real x, Real y, Real z) {
+    const int loc = ireg - G.voff;
+    int iz = fdiv(loc, G.mnxy, G.lnxy), ir = loc - iz * G.nxy, iy = fdiv(ir, G.mnx, G.lnx), ix = ir - iy * G.nx;
+    C t = dmin((C)x - (C)G.xb[ix], (C)G.xb[ix + 1] - (C)x);
+    t = dmin(t, dmin((C)y - (C)G.yb[iy], (C)G.yb[iy + 1] - (C)y));
+    t = dmin(t, dmin((C)z - (C)G.zb[iz], (C)G.zb[iz + 1] - (C)z));
+    return t;
+}
+// EGS_XYZGeometry::howfar (egs_nd_geometry.h:963-1104) with the face
+// distances in arithmetic type C; t is compared and returned in C.
+template <class C, class Real>
+__device__ inline int howfar_c(const Geom<Real> &G, int ireg, Real x, Real y, Real z, Real u, Real v, Real w, C &t,
+                               int &axis) {
+    const int loc = ireg - G.voff;
+    int iz = fdiv(loc, G.mnxy, G.lnxy), ir = loc - iz * G.nxy, iy = fdiv(ir, G.mnx, G.lnx), ix = ir - iy * G.nx;
+    int inew = ireg;
+    const C bt = (C)G.bt, hbt = (C)G.hbt;
+    if (u > 0) {
+        C d = ((C)G.xb[ix + 1] - (C)x) / (C)u;
+        if (d <= t) { t = (d <= bt) ? hbt : d; inew = (ix + 1 < G.nx) ? ireg + 1 : -1; axis = 0; }
+    } else if (u < 0) {
+        C d = ((C)G.xb[ix] - (C)x) / (C)u;
+        if (d <= t) { t = (d <= bt) ? hbt : d; inew = (ix - 1 >= 0) ? ireg - 1 : -1; axis = 0; }
+    }
+    if (v > 0) {
+        C d = ((C)G.yb[iy + 1] - (C)y) / (C)v;
+        if (d <= t) { t = (d <= bt) ? hbt : d; inew = (iy + 1 < G.ny) ? ireg + G.nx : -1; axis = 1; }
+    } else if (v < 0) {
+        C d = ((C)G.yb[iy] - (C)y) / (C)v;
+        if (d <= t) { t = (d <= bt) ? hbt : d; inew = (iy - 1 >= 0) ? ireg - G.nx : -1; axis = 1; }
+    }
+    if (w > 0) {
+        C d = ((C)G.zb[iz + 1] - (C)z) / (C)w;
+        if (d <= t) { t = (d <= bt) ? hbt : d; inew = (iz + 1 < G.nz) ? ireg + G.nxy : -1; axis = 2; }
+    } else if (w < 0) {
+        C d = ((C)G.zb[iz] - (C)z) / (C)w;
+        if (d <= t) { t = (d <= bt) ? hbt : d; inew = (iz - 1 >= 0) ? ireg - G.nxy : -1; axis = 2; }
+    }
+    return inew;
+}
+
+// The FP64 pieces of a `wide` step of the FP32 electron kernel, kept out of
+// line so that the FP32 step does not carry their registers.
+template <class Real>
+__device__ __noinline__ double wide_range(const Tables<Real> &T, const MedScalars<Real> &M, int qel, Real eke,
+                                          Real elke, int lelke, Real rhof) {
+    const Real *rr = rrow(T, M, lelke);
+    const double r0 = drange<double>(T, M, qel, (double)eke, (double)rr[0], lelke, (double)elke,
+                                     ((double)lelke - (double)M.eke0) / (double)M.eke1);
+    return (r0 + (double)rr[1 + qel]) / (double)rhof;
+}
+template <class Real>
+__device__ __noinline__ Real wide_hownear(const Geom<Real> &G, int ireg, Real x, Real y, Real z) {
+    return (Real)hownear_c<double>(G, ireg, x, y, z);
+}
+template <class Real>
+__device__ __noinline__ int wide_howfar(const Geom<Real> &G, int ireg, Real x, Real y, Real z, Real u, Real v, Real w,
+                                        Real &t, int &axis) {
+    double tw = t;
+    const int inew = howfar_c<double>(G, ireg, x, y, z, u, v, w, tw, axis);
+    t = (Real)tw;
+    return inew;
+}
+template <class Real>
+__device__ __noinline__ Real wide_eloss(const Tables<Real> &T, const MedScalars<Real> &M, int qel, double step, Real eke,
+                                        Real elke, int lelke, double range, Real rhof) {
+    return (Real)eloss_g<double>(T, M, qel, step, (double)eke, (double)elke, lelke, range, (double)rhof);
 }
 
 // Adj: adjoint replay of the continuous energy loss (see EList).
@@ -941,8 +1040,25 @@ __device__ inline Real eloss_g(const Tables<Real> &T, const MedScalars<Real> &M,
 // once at its end by mscat.  Its own instantiation, so that the EXACT kernels
 // carry none of this code.
 template <class Real, bool Multi, bool Adj = false, bool HFL = false, bool PI = false>
-__global__ void __launch_bounds__(MAX_BLOCK) k_electron(Params<Real> P) {
-    const Tables<Real> &T = P.T;
+__global__ void __launch_bounds__(MAX_BLOCK, sizeof(Real) == 4 && !Adj ? 6 : 1) k_electron(Params<Real> P) {
+    // The electron PWLF tables of every medium (etab: 16 coefficients per
+    // energy bin, erange: energy and ranges per bin; $SET INTERVAL/$EVALUATE,
+    // src/egsnrc.macros:1226-1262) are staged in shared memory when the launch
+    // gives room for them (P.esm_rows > 0): 16-byte vector copies, then every
+    // bin lookup of the step reads shared memory.
+    extern __shared__ __align__(16) unsigned char e_smem[];
+    Tables<Real> T = P.T;
+    if (P.esm_rows > 0) {
+        Real *se = (Real *)e_smem, *sr = se + (size_t)16 * P.esm_rows;
+        const int4 *ge4 = (const int4 *)P.T.etab, *gr4 = (const int4 *)P.T.erange;
+        int4 *se4 = (int4 *)se, *sr4 = (int4 *)sr;
+        const int ne = 16 * P.esm_rows * (int)sizeof(Real) / 16, nr = 4 * P.esm_rows * (int)sizeof(Real) / 16;
+        for (int i = threadIdx.x; i < ne; i += blockDim.x) se4[i] = ge4[i];
+        for (int i = threadIdx.x; i < nr; i += blockDim.x) sr4[i] = gr4[i];
+        __syncthreads();
+        T.etab = se;
+        T.erange = sr;
+    }
     const Geom<Real> &G = P.G;
     const unsigned lane = threadIdx.x & 31u;
     const unsigned nq = *P.ein.count < P.ein.capacity ? *P.ein.count : P.ein.capacity;
@@ -964,7 +1080,8 @@ __global__ void __launch_bounds__(MAX_BLOCK) k_electron(Params<Real> P) {
     // coefficients zero), so that its crossings also see the parent's path
     EList<Real> elstack[Adj ? LSTACK : 1];
     bool alive = false, exhausted = false;
-    unsigned long long nstep = 0, npush = 0, ninter = 0, lanes = 0, iters = 0;
+    unsigned long long nstep = 0, npush = 0, ninter = 0, lanes = 0, iters = 0, nwide = 0;
+    constexpr bool SPLIT = sizeof(Real) == 4 && !HFL;   // the FP32 kernels' FP64 steps (`wide`)
     int inter_wait = 0;   // warp-uniform iterations since the first lane became due
     double edep_tot = 0, esc_tot = 0;
     int err = 0;
@@ -1305,7 +1422,7 @@ __global__ void __launch_bounds__(MAX_BLOCK) k_electron(Params<Real> P) {
             const Real *rr = rrow(T, M, s.lelke);
             // range from the current energy to the lower edge of its bin
             // ($COMPUTE-DRANGE): serves both tstep and the residual range
-            const Real r0 = drange(T, M, qel, (Real)s.eke, rr[0], s.lelke, (Real)s.elke,
+            const Real r0 = drange<Real>(T, M, qel, (Real)s.eke, rr[0], s.lelke, (Real)s.elke,
                                    (s.lelke - (Real)M.eke0) / (Real)M.eke1);
             if (sig <= 0) { tstep = (Real)1e8; s.sig0 = (Real)1e-15; }
             else {
@@ -1316,11 +1433,11 @@ __global__ void __launch_bounds__(MAX_BLOCK) k_electron(Params<Real> P) {
                     else {
                         Real elkef = dlog(ekef);
                         int lelkef = min(max((int)((Real)M.eke1 * elkef + (Real)M.eke0), 1), s.lelke);
-                        if (lelkef == s.lelke) tstep = drange(T, M, qel, eke, ekef, s.lelke, elke, elkef);
+                        if (lelkef == s.lelke) tstep = drange<Real>(T, M, qel, eke, ekef, s.lelke, elke, elkef);
                         else {
                             const Real *rf = rrow(T, M, lelkef + 1);
                             Real ekei = rf[0], elkei = (lelkef + 1 - (Real)M.eke0) / (Real)M.eke1;
-                            tstep = drange(T, M, qel, ekei, ekef, lelkef, elkei, elkef);
+                            tstep = drange<Real>(T, M, qel, ekei, ekef, lelkef, elkei, elkef);
                             tstep = tstep + r0 + rr[1 + qel] - rf[1 + qel];
                         }
                     }
@@ -1341,6 +1458,20 @@ __global__ void __launch_bounds__(MAX_BLOCK) k_electron(Params<Real> P) {
             Real blccl = rhof * M.blcc;
             Real p2 = s.eke * (s.eke + 2 * rm), beta2 = p2 / (p2 + rm * rm);
             Real ssmfp = beta2 / blccl, skindepth = T.skindepth * ssmfp;
+            // Precision split of the FP32 kernels (egsgpu_config.fp64_near_faces):
+            // a step that starts within NEAR_FACE of a voxel face, or one that
+            // may reach the end of the range, is `wide`: its distance to the
+            // nearest face, its howfar distances, its residual range and its
+            // energy loss are computed in FP64 from the FP32 particle and table
+            // values.  Everything else stays FP32; the FP64 build is FP64
+            // throughout.
+            const bool wide = SPLIT && P.split && (tperp < (Real)NEAR_FACE || range <= dmin(tstep, tmxs));
+            double range_w = 0;
+            if (wide) {
+                tperp = wide_hownear(GP, p.ir, p.x, p.y, p.z);
+                range_w = wide_range(T, M, qel, (Real)s.eke, (Real)s.elke, s.lelke, (Real)rhof);
+                ++nwide;
+            }
             tustep = dmin(tustep, dmax(tperp, skindepth));
             bool callhowfar, dosingle = false, callmsdist, domultiple = false;
             Real ustep, uf, vf, wf, xf, yf, zf;
@@ -1388,7 +1519,11 @@ __global__ void __launch_bounds__(MAX_BLOCK) k_electron(Params<Real> P) {
             }
             const Real ustep0 = ustep;
             int irold = p.ir, irnew = p.ir, axis = -1;
-            if (callhowfar) irnew = HFL ? hfl_howfar(GP, p, ustep) : howfar(GP, p.ir, p.x, p.y, p.z, p.u, p.v, p.w, ustep, axis);
+            if (callhowfar) {
+                if (HFL) irnew = hfl_howfar(GP, p, ustep);
+                else if (wide) irnew = wide_howfar(GP, p.ir, p.x, p.y, p.z, p.u, p.v, p.w, ustep, axis);
+                else irnew = howfar(GP, p.ir, p.x, p.y, p.z, p.u, p.v, p.w, ustep, axis);
+            }
             if (Adj && irnew != irold && axis >= 0) {   // the step ends on a voxel face
                 const Real ua = axis == 0 ? p.u : (axis == 1 ? p.v : p.w);
                 const Real wa = (Real)P.wvox[irold], wb = irnew >= 0 ? (Real)P.wvox[irnew] : (Real)0;
@@ -1422,7 +1557,12 @@ __global__ void __launch_bounds__(MAX_BLOCK) k_electron(Params<Real> P) {
                     } else tvstep = tustep;
                 }
                 if (!PI && callhowfar && tvstep != tustep) dosingle = false;
-                de = eloss_g(T, M, qel, (Real)tvstep, (Real)s.eke, (Real)s.elke, s.lelke, range, (Real)rhof);
+                if (wide) {   // a step limited by the range ends it exactly, as in FP64
+                    const double tvw = (tvstep == range) ? range_w : (double)tvstep;
+                    de = wide_eloss(T, M, qel, tvw, (Real)s.eke, (Real)s.elke, s.lelke, range_w, (Real)rhof);
+                } else {
+                    de = eloss_g<Real>(T, M, qel, (Real)tvstep, (Real)s.eke, (Real)s.elke, s.lelke, range, (Real)rhof);
+                }
                 if (callmsdist) msdist_pII(T, M, p, s.eke, (Real)de, tustep, rhof, uf, vf, wf, xf, yf, zf, err);
                 Real edep = (Real)de, ekef = s.eke - edep;
                 if (!callmsdist) {
@@ -1522,8 +1662,10 @@ __global__ void __launch_bounds__(MAX_BLOCK) k_electron(Params<Real> P) {
         ninter += __shfl_down_sync(0xffffffffu, ninter, o);
         edep_tot += __shfl_down_sync(0xffffffffu, edep_tot, o);
         esc_tot += __shfl_down_sync(0xffffffffu, esc_tot, o);
+        if (SPLIT) nwide += __shfl_down_sync(0xffffffffu, nwide, o);
     }
     if (lane == 0) {
+        if (SPLIT) atomicAdd(P.counters + CNT_EWIDE, nwide);
         atomicAdd(P.counters + CNT_ELANES, lanes);
         atomicAdd(P.counters + CNT_EITER, iters);
         atomicAdd(P.counters + CNT_ESTEP, nstep);
@@ -1544,6 +1686,37 @@ __global__ void k_batch(double *d, double *sum, double *sum2, long long n) {
         sum[i] += x;
         sum2[i] += x * x;
         d[i] = 0;
+    }
+}
+
+// Geometry queries on one phantom through the transport kernels' own
+// functions (a checking aid): op 0 isWhere of x; op 1 howfar from region
+// ireg (howfarFromOut when ireg < 0) along u within t, writing the new region
+// and the distance; op 2 hownear of x in region ireg.  The host checks every
+// region index against the phantom before the launch.
+template <class Real>
+__global__ void k_geometry_query(Geom<Real> G, int op, long long n, const int *ireg, const double *x, const double *u,
+                                 double *t, int *inew) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double *p = x + 3 * i;
+    if (op == 0) {
+        int ix = plane_where(G.xb, G.nx, (Real)p[0]), iy = plane_where(G.yb, G.ny, (Real)p[1]);
+        int iz = plane_where(G.zb, G.nz, (Real)p[2]);
+        inew[i] = (ix >= 0 && iy >= 0 && iz >= 0) ? G.voff + ix + iy * G.nx + iz * G.nxy : -1;
+    } else if (op == 1) {
+        const double *d = u + 3 * i;
+        if (ireg[i] >= 0) {
+            Real tt = (Real)t[i];
+            inew[i] = howfar(G, ireg[i], (Real)p[0], (Real)p[1], (Real)p[2], (Real)d[0], (Real)d[1], (Real)d[2], tt);
+            t[i] = (double)tt;
+        } else {
+            double tt = t[i];
+            inew[i] = howfar_from_out(G, p, d, tt);
+            t[i] = tt;
+        }
+    } else {
+        t[i] = (double)hownear(G, ireg[i], (Real)p[0], (Real)p[1], (Real)p[2]);
     }
 }
 
@@ -1599,9 +1772,11 @@ struct EngineBase {
     virtual int read_totals(double *energy2, unsigned long long *counters, std::string &err) = 0;   // CNT_N counters
     virtual int restore_sums(const double *energy2, const unsigned long long *counters8, const double *sum,
                              const double *sum2, long long nv, std::string &err) = 0;
-    virtual int read_profile(double *out18, std::string &err) = 0;
+    virtual int read_profile(double *out20, std::string &err) = 0;
     virtual int history_tally(long long first, long long n, std::string &err) = 0;
     virtual int read_history_tally(double *out, std::string &err) = 0;
+    virtual int geometry_query(int op, long long n, const int *ireg, const double *x, const double *u, double *t,
+                               int *inew, std::string &err) = 0;
 };
 
 // The FP64 engine, built in its own translation unit (egs_transport_f64.cu).
@@ -1752,6 +1927,8 @@ struct Engine : EngineBase {
         out[15] = gexec ? 1.0 : 0.0;
         out[16] = c[CNT_PITER] ? (double)c[CNT_PLANES] / c[CNT_PITER] : 0.0;
         out[17] = c[CNT_EITER] ? (double)c[CNT_ELANES] / c[CNT_EITER] : 0.0;
+        out[18] = (double)c[CNT_EWIDE];
+        out[19] = 0.0;
         return 0;
     }
     int history_tally(long long first, long long n, std::string &err) override {
@@ -1768,9 +1945,40 @@ struct Engine : EngineBase {
         return 0;
     }
 
+    int geometry_query(int op, long long n, const int *ireg, const double *x, const double *u, double *t, int *inew,
+                       std::string &err) override {
+        if (!G.xb || nprob) { err = "a single geometry must be set"; return EGSGPU_ERR_STATE; }
+        if (op < 0 || op > 2 || n < 0 || !x || (op != 0 && (!ireg || !t)) || (op == 1 && !u) || (op != 2 && !inew)) {
+            err = "geometry query: bad arguments";
+            return EGSGPU_ERR_ARG;
+        }
+        if (n == 0) return 0;
+        if (op != 0)
+            for (long long i = 0; i < n; ++i)
+                if (ireg[i] >= nvox || (op == 2 && ireg[i] < 0)) { err = "geometry query: region out of range"; return EGSGPU_ERR_ARG; }
+        DevMem dreg, dx, du, dt, dnew;
+        CK(dreg.alloc(n * sizeof(int)));
+        CK(dx.alloc(3 * n * sizeof(double)));
+        CK(du.alloc(3 * n * sizeof(double)));
+        CK(dt.alloc(n * sizeof(double)));
+        CK(dnew.alloc(n * sizeof(int)));
+        CK(cudaMemcpy(dx.p, x, 3 * n * sizeof(double), cudaMemcpyHostToDevice));
+        if (op != 0) CK(cudaMemcpy(dreg.p, ireg, n * sizeof(int), cudaMemcpyHostToDevice));
+        if (op == 1) CK(cudaMemcpy(du.p, u, 3 * n * sizeof(double), cudaMemcpyHostToDevice));
+        if (op == 1) CK(cudaMemcpy(dt.p, t, n * sizeof(double), cudaMemcpyHostToDevice));
+        k_geometry_query<Real><<<(unsigned)((n + 255) / 256), 256>>>(G, op, n, (const int *)dreg.p, (const double *)dx.p,
+                                                                     (const double *)du.p, (double *)dt.p, (int *)dnew.p);
+        CK(cudaGetLastError());
+        CK(cudaDeviceSynchronize());
+        if (op != 0) CK(cudaMemcpy(t, dt.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+        if (op != 2) CK(cudaMemcpy(inew, dnew.p, n * sizeof(int), cudaMemcpyDeviceToHost));
+        return 0;
+    }
+
     int nmed = 0;
     std::vector<MedScalars<Real>> meds;
     DevMem d_etab, d_erange, d_gtab, d_pmax, d_ray, d_rayi, d_shell, d_shellat, d_elem, d_ms, d_msi;
+    int etab_rows = 0;   // electron PWLF bins over all media
     Tables<Real> T{};
     // geometry
     Geom<Real> G{};
@@ -1898,6 +2106,7 @@ struct Engine : EngineBase {
             return cudaMemcpy(d.p, src, bytes, cudaMemcpyHostToDevice);
         };
         CK(up(d_etab, etab.data(), etab.size() * sizeof(Real)));
+        etab_rows = (int)(etab.size() / 16);
         h_etab = etab;
         hatch_ = &H;
         CK(up(d_erange, erange.data(), erange.size() * sizeof(Real)));
@@ -2044,8 +2253,30 @@ struct Engine : EngineBase {
     cudaEvent_t ev_in = nullptr;
     bool graph_ok = true;
 
+    // Shared-memory staging of the electron PWLF tables: the bytes for `rows`
+    // bins of every medium (etab 16 + erange 4 values per bin).
+    static size_t esm_bytes(int rows) { return (size_t)rows * 20 * sizeof(Real); }
+    // Occupancy of an electron kernel and whether its tables are staged in
+    // shared memory: they are when they fit (egsgpu_config.smem_tables != -1)
+    // and staging keeps as many CTAs per SM resident as without it.
+    template <class K>
+    cudaError_t electron_shape(K kern, int bs, int &occ, int &rows) {
+        rows = 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, bs, 0);
+        if (e != cudaSuccess || cfg.smem_tables < 0) return e;
+        const int want = etab_rows;
+        const size_t bytes = esm_bytes(want);
+        if (want <= 0 || bytes > (size_t)SMEM_TABLES_MAX) return cudaSuccess;
+        if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes))) return e;
+        int occ_s = 0;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, kern, bs, bytes))) return e;
+        if (occ_s >= std::min(occ, cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm : occ)) { rows = want; occ = occ_s; }
+        return cudaSuccess;
+    }
+
     cudaError_t enqueue_rounds(const Params<Real> &P0, int gp, int ge, int bs, bool events, bool multi,
                                bool adj = false, bool hfl = false) {
+        const size_t esm = esm_bytes(P0.esm_rows);
         const bool pi = cfg.bca_algorithm == 1;
         unsigned *counts = (unsigned *)d_counts.p;
         cudaError_t e = cudaSuccess;
@@ -2063,12 +2294,12 @@ struct Engine : EngineBase {
             if ((e = cudaGetLastError())) break;
             if (events && (e = cudaEventRecord(gev[4 * r + 1], ws))) break;
             if (events && (e = cudaEventRecord(gev[4 * r + 2], ws))) break;
-            if (hfl) k_electron<Real, false, false, true><<<ge, bs, 0, ws>>>(P);
-            else if (pi && multi) k_electron<Real, true, false, false, true><<<ge, bs, 0, ws>>>(P);
-            else if (pi) k_electron<Real, false, false, false, true><<<ge, bs, 0, ws>>>(P);
-            else if (adj) k_electron<Real, false, true><<<ge, bs, 0, ws>>>(P);
-            else if (multi) k_electron<Real, true><<<ge, bs, 0, ws>>>(P);
-            else k_electron<Real, false><<<ge, bs, 0, ws>>>(P);
+            if (hfl) k_electron<Real, false, false, true><<<ge, bs, esm, ws>>>(P);
+            else if (pi && multi) k_electron<Real, true, false, false, true><<<ge, bs, esm, ws>>>(P);
+            else if (pi) k_electron<Real, false, false, false, true><<<ge, bs, esm, ws>>>(P);
+            else if (adj) k_electron<Real, false, true><<<ge, bs, esm, ws>>>(P);
+            else if (multi) k_electron<Real, true><<<ge, bs, esm, ws>>>(P);
+            else k_electron<Real, false><<<ge, bs, esm, ws>>>(P);
             if ((e = cudaGetLastError())) break;
             if (events && (e = cudaEventRecord(gev[4 * r + 3], ws))) break;
         }
@@ -2106,6 +2337,17 @@ struct Engine : EngineBase {
             std::string &err) override {
         if (nprob) { err = "the engine holds several phantoms; set one geometry first"; return EGSGPU_ERR_STATE; }
         return run_impl<false>(S, first, n, nbatch, seed, st, err);
+    }
+
+    // The device loops' iteration caps of this handle (egsgpu_config.loop_cap,
+    // .step_cap), written to the translation unit's constants before a run.
+    cudaError_t set_caps(cudaStream_t st) {
+        const int caps[2] = {cfg.loop_cap > 0 ? cfg.loop_cap : LOOP_CAP_DEFAULT,
+                             cfg.step_cap > 0 ? cfg.step_cap : STEP_CAP_DEFAULT};
+        cudaError_t e = cudaMemcpyToSymbolAsync(c_loop_cap, &caps[0], sizeof(int), 0, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_step_cap, &caps[1], sizeof(int), 0, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);   // the caps are read from host stack memory
+        return e;
     }
 
     // Histories of batch b of a run of n histories in nbatch batches
@@ -2158,19 +2400,20 @@ struct Engine : EngineBase {
             err = "PRESTA-I boundary crossing is for egsgpu_run and egsgpu_run_phantoms (no HOWFARLESS, no adjoint)";
             return EGSGPU_ERR_ARG;
         }
+        int esm_rows = 0;
         if (hfl) {
             if (int rc = hfl_tables(err)) return rc;
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, false, false, true>, bs, 0));
-            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, false, false, true>, bs, 0));
+            CK(electron_shape(k_electron<Real, false, false, true>, bs, occ_e, esm_rows));
         } else if (pi) {
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, Multi>, bs, 0));
-            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, Multi, false, false, true>, bs, 0));
+            CK(electron_shape(k_electron<Real, Multi, false, false, true>, bs, occ_e, esm_rows));
         } else if (adj) {
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, false, true>, bs, 0));
-            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, false, true>, bs, 0));
+            CK(electron_shape(k_electron<Real, false, true>, bs, occ_e, esm_rows));
         } else {
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, Multi>, bs, 0));
-            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, Multi>, bs, 0));
+            CK(electron_shape(k_electron<Real, Multi>, bs, occ_e, esm_rows));
         }
         const int cps_cap = cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm : 64;
         const int gp = sm_count * std::max(1, std::min(cps_cap, occ_p));
@@ -2189,6 +2432,8 @@ struct Engine : EngineBase {
         P.seed = seed;
         P.requeue_lanes = cfg.requeue_lanes > 0 ? cfg.requeue_lanes : 0;
         P.inter_batch = cfg.inter_batch > 0 ? std::min(cfg.inter_batch, 32) : (cfg.inter_batch < 0 ? 1 : 8);
+        P.esm_rows = esm_rows;
+        P.split = cfg.fp64_near_faces > 0 ? 1 : 0;
         if (Multi) {
             P.probs = (const Geom<Real> *)d_probs.p; P.pseeds = (const uint32_t *)d_pseeds.p;
             P.psrc = (const Source *)d_psrc.p; P.pvoff = (const int *)d_pvoff.p;
@@ -2208,6 +2453,7 @@ struct Engine : EngineBase {
         unsigned *counts = (unsigned *)d_counts.p;
         CK(cudaEventRecord(ev_in, st));
         CK(cudaStreamWaitEvent(ws, ev_in, 0));
+        CK(set_caps(ws));
         std::vector<long long> hprefix(nprob + 1), hfirst(nprob + 1);
         for (int b = 0; b < nbatch; ++b) {
             long long b0, bn;
@@ -2478,7 +2724,8 @@ struct Engine : EngineBase {
         const int bs = cfg.block_size > 0 ? cfg.block_size : 128;
         int occ_p = 1, occ_e = 1;
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, false>, bs, 0));
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, false>, bs, 0));
+        int esm_rows = 0;
+        CK(electron_shape(k_electron<Real, false>, bs, occ_e, esm_rows));
         const int cps_cap = cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm : 64;
         const int gp = sm_count * std::max(1, std::min(cps_cap, occ_p));
         const int ge = sm_count * std::max(1, std::min(cps_cap, occ_e));
@@ -2491,8 +2738,11 @@ struct Engine : EngineBase {
         P.seed = seed;
         P.requeue_lanes = 0;
         P.inter_batch = cfg.inter_batch > 0 ? std::min(cfg.inter_batch, 32) : (cfg.inter_batch < 0 ? 1 : 8);
+        P.esm_rows = esm_rows;
+        P.split = cfg.fp64_near_faces > 0 ? 1 : 0;
         // the array keeps the previous call's contents: clear the counters
         CK(cudaMemsetAsync(scratch, 0, 1024, st));
+        CK(set_caps(st));
         CK(cudaMemsetAsync(dose, 0, (size_t)nvox * sizeof(double), st));
         P.pout = Q[0]; P.eout = Q[2]; P.pin = Q[0]; P.ein = Q[2];
         k_source<Real, false><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(P, S, first, n);
@@ -2506,7 +2756,7 @@ struct Engine : EngineBase {
             P.pin = Q[cur]; P.ein = Q[2 + cur]; P.pout = Q[nxt]; P.eout = Q[2 + nxt];
             k_photon<Real, false><<<gp, bs, 0, st>>>(P);
             CK(cudaGetLastError());
-            k_electron<Real, false><<<ge, bs, 0, st>>>(P);
+            k_electron<Real, false><<<ge, bs, esm_bytes(esm_rows), st>>>(P);
             CK(cudaGetLastError());
             unsigned h[9];
             CK(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, st));
@@ -3047,6 +3297,13 @@ int egsgpu_get_history_tally(egsgpu_handle *h, double *out) {
     return h->eng->read_history_tally(out, h->err);
 }
 
+int egsgpu_geometry_query(egsgpu_handle *h, int op, long long n, const int32_t *ireg, const double *x,
+                          const double *u, double *t, int32_t *inew) {
+    if (!h) return EGSGPU_ERR_ARG;
+    if (!h->have_geom) { h->err = "geometry not set"; return EGSGPU_ERR_STATE; }
+    return h->eng->geometry_query(op, n, ireg, x, u, t, inew, h->err);
+}
+
 // Checkpoint layout: magic, nvox, nhist, nbatch, energy[2], counters[8], sum[nvox], sum2[nvox]
 int egsgpu_checkpoint(egsgpu_handle *h, void *buf, size_t *size) {
     if (!h || !size || !h->have_geom) return EGSGPU_ERR_ARG;
@@ -3090,6 +3347,50 @@ int egsgpu_restore(egsgpu_handle *h, const void *buf, size_t size) {
     if (rc) return rc;
     h->nhist = hdr[2];
     h->nbatch = (int)hdr[3];
+    return 0;
+}
+
+// Host-only: the checkpoint of the union of two runs of the same phantom
+// (the .egsdat combine of egs_application.cpp:624-660, addState): histories,
+// batches, energy totals, counters and the per-voxel batch sums and sums of
+// squares add.  Batch-wise uncertainties need equal histories per batch, so
+// shards whose histories per batch differ are refused.
+int egsgpu_combine_checkpoints(const void *a, size_t na, const void *b, size_t nb, void *out, size_t *nout) {
+    if (!a || !b || !nout || na < 112 || nb < 112) return EGSGPU_ERR_ARG;
+    long long ha[4], hb[4];
+    std::memcpy(ha, a, 32);
+    std::memcpy(hb, b, 32);
+    const long long magic = 0x45475347505531LL;
+    if (ha[0] != magic || hb[0] != magic || ha[1] != hb[1] || ha[1] < 0) return EGSGPU_ERR_ARG;
+    const long long nv = ha[1];
+    const size_t need = 8 * 4 + 2 * 8 + 8 * 8 + 2 * (size_t)nv * 8;
+    if (na < need || nb < need) return EGSGPU_ERR_ARG;
+    if (!out) { *nout = need; return 0; }
+    if (*nout < need) { *nout = need; return EGSGPU_ERR_ARG; }
+    if (ha[3] > 0 && hb[3] > 0 && ha[2] * hb[3] != hb[2] * ha[3]) return EGSGPU_ERR_ARG;
+    const char *pa = (const char *)a, *pb = (const char *)b;
+    char *po = (char *)out;
+    long long ho[4] = {magic, nv, ha[2] + hb[2], ha[3] + hb[3]};
+    std::memcpy(po, ho, 32);
+    double ea[2], eb[2];
+    std::memcpy(ea, pa + 32, 16);
+    std::memcpy(eb, pb + 32, 16);
+    ea[0] += eb[0];
+    ea[1] += eb[1];
+    std::memcpy(po + 32, ea, 16);
+    unsigned long long ca[8], cb[8];
+    std::memcpy(ca, pa + 48, 64);
+    std::memcpy(cb, pb + 48, 64);
+    for (int k = 0; k < 8; ++k) ca[k] += cb[k];
+    std::memcpy(po + 48, ca, 64);
+    for (long long i = 0; i < 2 * nv; ++i) {
+        double x, y;
+        std::memcpy(&x, pa + 112 + 8 * i, 8);
+        std::memcpy(&y, pb + 112 + 8 * i, 8);
+        x += y;
+        std::memcpy(po + 112 + 8 * i, &x, 8);
+    }
+    *nout = need;
     return 0;
 }
 

@@ -72,6 +72,26 @@ typedef struct {
                              default from the lowest ECUT (:2794-2815).  PRESTA-I
                              is for egsgpu_run and egsgpu_run_phantoms (not with
                              HOWFARLESS, the adjoint or egsgpu_run_noalloc). */
+    int loop_cap;         /* iterations after which a device rejection loop is
+                             abandoned; 0 = default (100000).  The reference's
+                             analogues: the 100000-try limit of
+                             simulateSingleShower (egs++/egs_application.cpp:
+                             925-930) and loopMax (egs++/egs_functions.h:96) */
+    int step_cap;         /* transport steps after which a particle is abandoned;
+                             0 = default (2^22).  Either cap, once reached, makes
+                             the run return EGSGPU_ERR_LOOP (the caps are set on
+                             the device before each run: handles on one device
+                             whose runs overlap share the last caps set) */
+    int smem_tables;      /* electron PWLF tables (every medium's etab and range
+                             rows) staged in shared memory by the electron kernel
+                             when they fit without lowering its occupancy: 0 =
+                             default (staged), -1 = read from global memory
+                             (results are identical either way) */
+    int fp64_near_faces;  /* FP32 transport only: 1 computes the electron steps
+                             that start within 2^-12 cm of a voxel face or may end
+                             the range in FP64 (distances to the faces, residual
+                             range, energy loss); 0 = default (FP32 throughout;
+                             FP64 dose tallies either way) */
 } egsgpu_config;
 
 /* Source: egs++ EGS_ParallelBeam (sources/egs_parallel_beam) with a point
@@ -224,11 +244,29 @@ int egsgpu_adjoint(egsgpu_handle *h, long long first, long long n, uint32_t seed
 int egsgpu_set_history_tally(egsgpu_handle *h, long long first, long long n);
 int egsgpu_get_history_tally(egsgpu_handle *h, double *out);
 
-/* Device-side profile of the runs since the last reset: out[18] =
+/* Geometry queries on the handle's phantom (set by egsgpu_set_xyz_geometry),
+ * computed on the GPU by the transport kernels' own geometry functions in the
+ * handle's precision.  A checking aid: each op is the EGS_XYZGeometry method
+ * it replaces (egs++/geometry/egs_nd_geometry/egs_nd_geometry.h):
+ *   op 0  isWhere (:791-805): inew[i] = region of point x[3i..3i+2], -1 outside;
+ *   op 1  howfar (:963-1104), or howfarFromOut (:1281-1379) when ireg[i] < 0:
+ *         from region ireg[i] at x along unit direction u[3i..3i+2] within
+ *         t[i]; inew[i] = region entered (ireg[i] when no face is within t[i],
+ *         -1 when leaving), t[i] = the distance (in/out);
+ *   op 2  hownear (:1106-1122): t[i] = distance from x to the nearest face of
+ *         region ireg[i] (>= 0).
+ * Arrays of the ops that do not use them may be NULL; region indices beyond
+ * the phantom are EGSGPU_ERR_ARG. */
+int egsgpu_geometry_query(egsgpu_handle *h, int op, long long n, const int32_t *ireg, const double *x,
+                          const double *u, double *t, int32_t *inew);
+
+/* Device-side profile of the runs since the last reset: out[20] =
  * {ms source, ms photon, ms electron, ms batch, launches of each (4),
  *  photon steps, electron steps, photon-kernel pushes, electron-kernel pushes,
  *  photon interactions, electron interactions, autotuned chunk, graph in use,
- *  mean busy lanes per warp iteration in the photon and electron kernels};
+ *  mean busy lanes per warp iteration in the photon and electron kernels,
+ *  electron steps of the FP32 build computed in FP64 near a voxel face or
+ *  the end of the range, 0};
  * times are CUDA-event
  * durations on the launch stream.  No counterpart in the reference API
  * (the reference reports CPU time per batch, egs++/egs_timer.cpp). */
@@ -239,6 +277,17 @@ int egsgpu_get_profile(egsgpu_handle *h, double *out);
  * (egs++/egs_application.cpp:482-560). `size` is in/out. */
 int egsgpu_checkpoint(egsgpu_handle *h, void *buf, size_t *size);
 int egsgpu_restore(egsgpu_handle *h, const void *buf, size_t size);
+
+/* Combines the checkpoints of two shards of one problem (same phantom,
+ * disjoint history ranges or seeds) into the checkpoint of their union:
+ * histories, batches, energy totals, counters and the per-voxel batch sums
+ * and sums of squares add, as the reference sums parallel jobs' .egsdat files
+ * (egs++/egs_application.cpp:624-660, combineResults/addState).  Host only:
+ * needs no GPU and no handle.  Shards with different histories per batch are
+ * EGSGPU_ERR_ARG (batch-wise uncertainties need equal batches).  out may be
+ * NULL to query *nout; `out` may alias `a`.  Restore the result with
+ * egsgpu_restore to read doses. */
+int egsgpu_combine_checkpoints(const void *a, size_t na, const void *b, size_t nb, void *out, size_t *nout);
 
 /* No-allocation transport, for callers that may not allocate device memory
  * while they run: a real-time loop that must not block on the allocator, or a

@@ -22,12 +22,18 @@
 // The tables come from the host data layer (egsnrc_gb300/csrc/egs_hatch.cpp),
 // whose values are pinned separately against the raw data files.
 //
-// Pinning: the RANMAR generator is pinned to the one golden vector the
-// reference ships for this path (user_codes/ranmar_test).  Transport physics
-// parity is UNPINNED: the reference has no transport, dose or cross-section
-// golden values, and its transport core (Mortran3 -> Fortran 77) cannot be
-// compiled without a Fortran compiler, so no reference run checks this
-// restatement.
+// Pinning (the reference has no transport, dose or cross-section golden
+// values, and its transport core, Mortran3 -> Fortran 77, cannot be compiled
+// here without a Fortran compiler):
+//   - RANMAR against the one golden vector the reference ships for this path
+//     (user_codes/ranmar_test);
+//   - the transport against a run of the reference itself, BEAMnrc's EXslabs
+//     example: its listing and exit phase space (tests/test_oracle_exslabs.py);
+//   - the XYZ geometry bit for bit, and the parallel-beam source and spectrum
+//     in distribution, against the reference's own egs++ classes compiled from
+//     its sources (oracle/egspp_ref.cpp, tests/test_egspp_reference.py);
+//   - the Klein-Nishina, Sauter and Bethe-Heitler samplers against their
+//     analytic distributions (tests/test_oracle_samplers.py).
 //
 // Random numbers: either one RANMAR stream for the whole run (as the
 // reference does) or Philox-4x32-10 (Salmon et al., SC'11) with one stream
@@ -271,15 +277,18 @@ double hownear(const Geometry &G, int ireg, const Particle &p) {   // egs_nd_geo
     return t;
 }
 
+// EGS_PlanesT::isWhere + EGS_BaseGeometry::findRegion (egs_planes.h:301-311,
+// egs_base_geometry.h:178-190): b[hi-1] < x <= b[hi], so a point on an
+// interior plane belongs to the slab below it.
 int plane_where(const std::vector<double> &b, double x) {
     int n = (int)b.size() - 1;
     if (x < b[0] || x > b[n]) return -1;
-    int lo = 0, hi = n;   // b[lo] <= x < b[hi]
+    int lo = 0, hi = n;
     while (hi - lo > 1) {
         int mid = (lo + hi) / 2;
-        if (x < b[mid]) hi = mid; else lo = mid;
+        if (x <= b[mid]) hi = mid; else lo = mid;
     }
-    return lo;
+    return hi - 1;
 }
 
 int is_where(const Geometry &G, double x, double y, double z) {
@@ -441,11 +450,10 @@ int howfar_from_out(const Geometry &G, Particle &p, double &t) {
             }
             if (ok) {
                 int inew = idx[0] + idx[1] * G.nx + idx[2] * G.nxy;
-                if (t1 < G.bt) {
+                if (t1 < G.bt) {   // howfar may shorten t1 (egs_nd_geometry.h:1303-1308)
                     Particle tp = p; tp.x = q[0]; tp.y = q[1]; tp.z = q[2];
-                    double tt = t1;
-                    int itest = howfar(G, inew, tp, tt);
-                    if (itest == -1 && tt < G.bt) return -1;
+                    int itest = howfar(G, inew, tp, t1);
+                    if (itest == -1 && t1 < G.bt) return -1;
                 }
                 t = t1;
                 return inew;
@@ -516,7 +524,10 @@ void rayleigh_sample(Run &R, Particle &p, const Medium &m, const PhotonCtx &pc, 
 // COMPT, bound Compton with resampling (ibcmp = 3), egsnrc.mortran:528-805.
 // Returns the local binding-energy deposition; fills the scattered photon
 // (in place) and the electron.
-double compton(Run &R, Particle &p, const Medium &m, Particle &el) {
+// With bound = false, Klein-Nishina scattering on free electrons (the
+// ibcmp = 0 path of COMPT, :552-640 without the shell and pz sampling); used
+// by the tests of the Klein-Nishina sampler alone.
+double compton(Run &R, Particle &p, const Medium &m, Particle &el, bool bound = true) {
     const Hatch &H = R.O->H;
     double peig = p.E, ko = peig / RM, broi = 1 + 2 * ko;
     bool first_time = true;
@@ -524,7 +535,7 @@ double compton(Run &R, Particle &p, const Medium &m, Particle &el) {
     double alph1 = 0, alph2 = 0, alpha = 0, bro = 0, broi2 = 0, bro1 = 0, rejmax = 0;
     int j = 0;
 resample:
-    {
+    if (bound) {
         double r17 = rnd(R, p);
         r17 = 1 + r17 * m.n_shell;
         int i = (int)r17;
@@ -565,7 +576,7 @@ resample_kn:
     first_time = false;
     if (br < bro || br > 1) goto resample_kn;
     costhe = 1 - temp;
-    {
+    if (bound) {
         double br2 = br * br, aux = ko * (ko - Uj) * temp, aux1 = 2 * aux + Uj * Uj;
         double pzmax = aux - Uj;
         if (pzmax < 0 && pzmax * pzmax >= aux1) goto resample;
@@ -1594,9 +1605,10 @@ bool source_particle(Run &R, uint32_t hist, Particle &p) {
     p.E = (p.iq == 0) ? ek : ek + RM;
     p.x = x; p.y = y; p.z = z;
     p.u = u; p.v = v; p.w = w;
+    // EGS_Application::simulateSingleShower (egs_application.cpp:938-945)
     int ir = is_where(R.O->G, x, y, z);
     if (ir < 0) {
-        double t = 1e10;
+        double t = 1e30;   // veryFar, egs_functions.h:105
         ir = howfar_from_out(R.O->G, p, t);
         if (ir >= 0) { p.x += p.u * t; p.y += p.v * t; p.z += p.w * t; }
     }
@@ -1689,6 +1701,121 @@ int oracle_set_geometry(oracle_handle *h, int nx, int ny, int nz, const double *
         if (G.med[i] < 0 || G.med[i] >= (int)h->O.H.media.size()) return 1;
     h->T.batch.assign(nv, 0); h->T.sum.assign(nv, 0); h->T.sum2.assign(nv, 0);
     return 0;
+}
+
+// Geometry queries on the current phantom, as egsgpu_geometry_query: op 0
+// isWhere, op 1 howfar (howfarFromOut for ireg < 0), op 2 hownear.
+int oracle_geometry_query(oracle_handle *h, int op, long long n, const int32_t *ireg, const double *x,
+                          const double *u, double *t, int32_t *inew) {
+    const Geometry &G = h->O.G;
+    const long long nv = (long long)G.nxy * G.nz;
+    for (long long i = 0; i < n; ++i) {
+        Particle p;
+        p.x = x[3 * i]; p.y = x[3 * i + 1]; p.z = x[3 * i + 2];
+        if (op == 0) {
+            inew[i] = is_where(G, p.x, p.y, p.z);
+        } else if (op == 1) {
+            p.u = u[3 * i]; p.v = u[3 * i + 1]; p.w = u[3 * i + 2];
+            if (ireg[i] >= nv) return 1;
+            inew[i] = ireg[i] >= 0 ? howfar(G, ireg[i], p, t[i]) : howfar_from_out(G, p, t[i]);
+        } else if (op == 2) {
+            if (ireg[i] < 0 || ireg[i] >= nv) return 1;
+            t[i] = hownear(G, ireg[i], p);
+        } else {
+            return 1;
+        }
+    }
+    return 0;
+}
+
+// Interaction samplers alone, for the distribution tests: n interactions of
+// a photon (or, for kind 2, a photo-electron) of energy E in medium `med`,
+// on history streams first, first+1, ...:
+//   kind 0  Klein-Nishina on free electrons: out = {k'/k, cos theta of the photon}
+//   kind 1  bound Compton (ibcmp = 3):        out = {k'/k, cos theta, binding energy}
+//   kind 2  photo-electron direction ($SELECT-PHOTOELECTRON-DIRECTION) of a
+//           photo-electron of total energy E: out = {cos theta}
+//   kind 3  pair production:                  out = {electron total energy, positron total energy}
+// out has 3 values per interaction (unused ones 0).
+int oracle_sample_interaction(oracle_handle *h, int kind, int med, double E, long long n, uint32_t seed,
+                              double *out) {
+    Tally T;
+    Run R;
+    R.O = &h->O; R.T = &T; R.ranmar = false; R.seed = seed;
+    if (med < 0 || med >= (int)h->O.H.media.size()) return 1;
+    const Medium &m = h->O.H.media[med];
+    for (long long i = 0; i < n; ++i) {
+        Particle p;
+        p.hist = (uint32_t)i; p.sid = 0; p.n = 0; p.cache_blk = -1; p.wt = 1;
+        p.x = p.y = p.z = 0; p.u = 0; p.v = 0; p.w = 1; p.ir = 0;
+        p.iq = kind == 2 ? -1 : 0;
+        p.E = E;
+        double *o = out + 3 * i;
+        o[0] = o[1] = o[2] = 0;
+        if (kind == 0 || kind == 1) {
+            Particle el;
+            double uj = compton(R, p, m, el, kind == 1);
+            o[0] = p.E / E; o[1] = p.w; o[2] = uj;
+        } else if (kind == 2) {
+            // the direction part of PHOTO for a photo-electron of total energy E
+            double eelec = E, beta = std::sqrt((eelec - RM) * (eelec + RM)) / eelec, gamma = eelec / RM;
+            double alpha = 0.5 * gamma - 0.5 + 1. / gamma, ratio = beta / alpha, costhe, sinth2, xi;
+            while (true) {
+                double rn = rnd(R, p);
+                rn = 2. * rn - 1.;
+                if (ratio <= 0.2) {
+                    double fk = rn + 0.5 * ratio * (1. - rn) * (1. + rn);
+                    if (gamma < 100) costhe = (beta + fk) / (1. + beta * fk);
+                    else if (fk > 0) costhe = 1 - (1 - fk) * (gamma - 3) / (2 * (1 + fk) * (gamma - 1) * (gamma - 1) * (gamma - 1));
+                    else costhe = (beta + fk) / (1. + beta * fk);
+                    xi = (1 + beta * fk) * gamma * gamma;
+                } else {
+                    xi = gamma * gamma * (1. + alpha * (std::sqrt(1. + ratio * (2. * rn + ratio)) - 1.));
+                    costhe = (1. - 1. / xi) / beta;
+                }
+                sinth2 = std::max(0., (1. - costhe) * (1. + costhe));
+                double rn2 = rnd(R, p);
+                if (!(rn2 > 0.5 * (1. + gamma) * sinth2 * xi / gamma)) break;
+            }
+            o[0] = costhe;
+        } else if (kind == 3) {
+            Particle second;
+            pair(R, p, m, second);
+            o[0] = p.iq < 0 ? p.E : second.E;
+            o[1] = p.iq < 0 ? second.E : p.E;
+        } else {
+            return 1;
+        }
+    }
+    return R.errors ? 2 : 0;
+}
+
+// Pair-production constants of medium `med` (HATCH, from PEGS4): out[51] =
+// {dl1..dl6 for l = 0..7 (dl[k][l] at 8 k + l), delcm, bpar[0], bpar[1]}.
+int oracle_medium_pair(oracle_handle *h, int med, double *out) {
+    if (med < 0 || med >= (int)h->O.H.media.size()) return 1;
+    const Medium &m = h->O.H.media[med];
+    for (int k = 0; k < 6; ++k)
+        for (int l = 0; l < 8; ++l) out[8 * k + l] = m.dl[k][l];
+    out[48] = m.delcm; out[49] = m.bpar[0]; out[50] = m.bpar[1];
+    return 0;
+}
+
+// The source particles of histories [first, first+n) as they enter the
+// phantom: out[9 i ...] = {charge, kinetic energy, x, y, z, u, v, w, region}
+// (region -1 for a particle that misses; its position is then the source's).
+int oracle_sample_source(oracle_handle *h, long long first, long long n, uint32_t seed, double *out) {
+    Tally T;
+    Run R;
+    R.O = &h->O; R.T = &T; R.ranmar = false; R.seed = seed;
+    for (long long i = 0; i < n; ++i) {
+        Particle p;
+        source_particle(R, (uint32_t)(first + i), p);
+        double *o = out + 9 * i;
+        o[0] = p.iq; o[1] = p.iq == 0 ? p.E : p.E - RM;
+        o[2] = p.x; o[3] = p.y; o[4] = p.z; o[5] = p.u; o[6] = p.v; o[7] = p.w; o[8] = p.ir;
+    }
+    return R.errors ? 1 : 0;
 }
 
 // HOWFARLESS transport (on != 0) in the current, homogeneous phantom: call

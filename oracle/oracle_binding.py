@@ -9,19 +9,36 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 LIB_PATH = os.path.join(HERE, "liboracle.so")
+# the same restatement built for speed (-O3 -ffast-math, the reference's own
+# Fortran flags); the CPU-baseline timings of bench.py use it, the parity
+# checks use LIB_PATH (no contraction, rounding like the GPU's FP64 build)
+FAST_LIB_PATH = os.path.join(HERE, "liboracle_fast.so")
 DATA_DIR = os.path.join(ROOT, "egsnrc_gb300", "data")
 PEGS_FILE = os.path.join(DATA_DIR, "521icru.pegs4dat")
 
 _L = None
+_LF = None
 
 
-def lib():
-    global _L
+def lib(fast=False):
+    global _L, _LF
+    if fast:
+        if _LF is None:
+            if not os.path.exists(FAST_LIB_PATH):
+                import subprocess
+                subprocess.run(["make", "-s", "liboracle_fast.so"], cwd=HERE, check=True)
+            _LF = _declare(C.CDLL(FAST_LIB_PATH))
+        return _LF
     if _L is None:
         if not os.path.exists(LIB_PATH):
             import subprocess
             subprocess.run(["make", "-s"], cwd=HERE, check=True)
-        L = C.CDLL(LIB_PATH)
+        _L = _declare(C.CDLL(LIB_PATH))
+    return _L
+
+
+def _declare(L):
+    if True:   # argument types of every exported function
         vp, dp, i64 = C.c_void_p, C.POINTER(C.c_double), C.c_longlong
         L.oracle_create.restype = vp
         L.oracle_create.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(C.c_char_p), C.c_int, C.c_double, C.c_double]
@@ -54,8 +71,11 @@ def lib():
         L.oracle_kn_sigma0.argtypes = [C.c_double]
         L.oracle_photon_xsec.argtypes = [vp, C.c_int, C.c_double, dp]
         L.oracle_electron_xsec.argtypes = [vp, C.c_int, C.c_double, dp]
-        _L = L
-    return _L
+        L.oracle_geometry_query.argtypes = [vp, C.c_int, i64, vp, vp, vp, vp, vp]
+        L.oracle_sample_source.argtypes = [vp, i64, i64, C.c_uint32, dp]
+        L.oracle_sample_interaction.argtypes = [vp, C.c_int, C.c_int, C.c_double, i64, C.c_uint32, dp]
+        L.oracle_medium_pair.argtypes = [vp, C.c_int, dp]
+    return L
 
 
 def _dp(a):
@@ -63,10 +83,12 @@ def _dp(a):
 
 
 class Oracle:
-    def __init__(self, media, ecut=0.521, pcut=0.010, pegs_file=PEGS_FILE, bca_algorithm=0, skindepth=3.0):
+    def __init__(self, media, ecut=0.521, pcut=0.010, pegs_file=PEGS_FILE, bca_algorithm=0, skindepth=3.0,
+                 fast=False):
         """bca_algorithm 0: EXACT boundary crossing, 1: PRESTA-I (with
-        skindepth <= 1e-4 the old PRESTA default skin depth)."""
-        L = lib()
+        skindepth <= 1e-4 the old PRESTA default skin depth).  fast: the
+        build for timing (FAST_LIB_PATH)."""
+        L = lib(fast)
         names = (C.c_char_p * len(media))(*[m.encode() for m in media])
         h = L.oracle_create_bca(DATA_DIR.encode(), pegs_file.encode(), names, len(media), ecut, pcut,
                                 int(bca_algorithm), float(skindepth))
@@ -139,6 +161,45 @@ class Oracle:
         out = np.zeros(self._hist_n)
         self.L.oracle_get_history_tally(self.h, _dp(out))
         return out
+
+    def geometry_query(self, op, ireg=None, x=None, u=None, t=None):
+        """isWhere (op 0), howfar (op 1; howfarFromOut where ireg < 0) and
+        hownear (op 2) on the current phantom, as egsgpu_geometry_query."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        n = len(x)
+        ireg = np.ascontiguousarray(ireg if ireg is not None else np.zeros(n), dtype=np.int32)
+        u = np.ascontiguousarray(u if u is not None else np.zeros((n, 3)), dtype=np.float64)
+        t = np.array(t if t is not None else np.zeros(n), dtype=np.float64)
+        inew = np.zeros(n, dtype=np.int32)
+        rc = self.L.oracle_geometry_query(self.h, int(op), n, ireg.ctypes.data, x.ctypes.data, u.ctypes.data,
+                                          t.ctypes.data, inew.ctypes.data)
+        if rc:
+            raise RuntimeError("oracle geometry query: bad arguments")
+        return inew, t
+
+    def sample_source(self, n, seed=1, first=0):
+        """Source particles of histories [first, first+n) as they enter the
+        phantom: rows of charge, kinetic energy, x, y, z, u, v, w, region."""
+        out = np.zeros((n, 9))
+        if self.L.oracle_sample_source(self.h, int(first), int(n), int(seed), _dp(out)):
+            raise RuntimeError("oracle source sampling error")
+        return out
+
+    def sample_interaction(self, kind, med, energy, n, seed=1):
+        """n samples of one interaction sampler alone (kind 0 Klein-Nishina on
+        free electrons, 1 bound Compton, 2 photo-electron direction, 3 pair);
+        rows of 3 values as oracle_sample_interaction describes."""
+        out = np.zeros((n, 3))
+        rc = self.L.oracle_sample_interaction(self.h, int(kind), int(med), float(energy), int(n), int(seed), _dp(out))
+        if rc:
+            raise RuntimeError("oracle sampler error %d" % rc)
+        return out
+
+    def pair_constants(self, med):
+        """dl[6][8], delcm and bpar[2] of medium med."""
+        out = np.zeros(51)
+        assert self.L.oracle_medium_pair(self.h, int(med), _dp(out)) == 0
+        return out[:48].reshape(6, 8), out[48], out[49:51]
 
     def photon_xsec(self, med, e):
         out = np.zeros(4)

@@ -57,3 +57,39 @@ def test_null_handle_calls_fail_cleanly(L):
     assert L.egsgpu_run(None, 0, 10, 1, 1, None) == 1
     assert L.egsgpu_get_tallies(None, None, None, None) == 7
     assert L.egsgpu_last_error(None) == b"null handle"
+
+
+def blob(nv, hist, batches, sums, sum2s, dep=1.0, esc=2.0):
+    """A checkpoint in the layout egsgpu_checkpoint writes."""
+    import numpy as np
+    hdr = np.array([0x45475347505531, nv, hist, batches], dtype=np.int64).tobytes()
+    en = np.array([dep, esc], dtype=np.float64).tobytes()
+    cnt = np.arange(8, dtype=np.uint64).tobytes()
+    return hdr + en + cnt + np.asarray(sums, np.float64).tobytes() + np.asarray(sum2s, np.float64).tobytes()
+
+
+def test_combine_checkpoints_adds_shards(L):
+    import numpy as np
+    rng = np.random.default_rng(1)
+    nv = 37
+    a = blob(nv, 1000, 10, rng.random(nv), rng.random(nv), 5.0, 1.0)
+    b = blob(nv, 500, 5, rng.random(nv), rng.random(nv), 3.0, 2.0)
+    c = eg.checkpoint_arrays(eg.combine_checkpoints(a, b))
+    A, B = eg.checkpoint_arrays(a), eg.checkpoint_arrays(b)
+    assert c["histories"] == 1500 and c["batches"] == 15
+    assert c["deposited"] == 8.0 and c["escaped"] == 3.0
+    assert np.array_equal(c["counters"], 2 * np.arange(8, dtype=np.uint64))
+    assert np.array_equal(c["sum"], A["sum"] + B["sum"]) and np.array_equal(c["sum2"], A["sum2"] + B["sum2"])
+
+
+def test_combine_checkpoints_refuses_mismatches(L):
+    import numpy as np
+    a = blob(4, 100, 10, np.ones(4), np.ones(4))
+    with pytest.raises(eg.EGSError):              # another phantom size
+        eg.combine_checkpoints(a, blob(5, 100, 10, np.ones(5), np.ones(5)))
+    with pytest.raises(eg.EGSError):              # other histories per batch
+        eg.combine_checkpoints(a, blob(4, 100, 5, np.ones(4), np.ones(4)))
+    with pytest.raises(eg.EGSError):              # truncated
+        eg.combine_checkpoints(a, a[:-8])
+    n = C.c_size_t(0)
+    assert L.egsgpu_combine_checkpoints(a, len(a), a, len(a), None, C.byref(n)) == 0 and n.value == len(a)

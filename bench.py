@@ -449,7 +449,10 @@ def batched_measure(args, ws, rank, local, dist, K, Wm, no_cpu, fp64_frac):
             "e2e": {"value": H * ws * K / Te, "unit": "histories/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(2 * nv_all * 8 + 64),
                     "path": "egsgpu_set_phantoms + egsgpu_run_phantoms + egsgpu_get_tallies"},
-            "roofline": roof, "gpu_launches": int(launches)}
+            "roofline": roof, "gpu_launches": int(launches),
+            "autotuner": {"chunk": prof["chunk"], "launch_shape": prof["launch_shape"],
+                          "shapes": "threads per CTA / CTAs per SM of photon, electron kernels relative to the "
+                                    "most that fit: 0 128/0/0, 1 64/0/0, 2 96/0/0, 3 128/0/-1, 4 128/-2/0, 5 64/0/-2"}}
     if rank == 0 and not args.no_fp64:
         # the same phantoms one after another (egsgpu_run per phantom): FP32, and the plain FP64 form
         for prec, key, frac in ((args.precision, "one_at_a_time", 1.0), (64, "fp64_one_at_a_time", fp64_frac)):
@@ -633,6 +636,23 @@ def main():
     s, s2, tot = eng.tallies()
     sig, nsel = sigma_eff(s, s2, K) if K > 1 else (None, 0)
     value = H * ws * K / T
+    combined = None
+    if dist:
+        # the ranks' shards of one problem combine into one result
+        # (egsgpu_combine_checkpoints, the .egsdat combine)
+        blobs = [None] * ws
+        dist.all_gather_object(blobs, eng.checkpoint())
+        if rank == 0:
+            comb = blobs[0]
+            for b in blobs[1:]:
+                comb = eg.combine_checkpoints(comb, b)
+            c = eg.checkpoint_arrays(comb)
+            parts = [eg.checkpoint_arrays(b) for b in blobs]
+            assert c["histories"] == H * K * ws and c["batches"] == K * ws
+            assert abs(c["deposited"] - sum(x["deposited"] for x in parts)) <= 1e-9 * c["deposited"]
+            csig, cn = sigma_eff(c["sum"], c["sum2"], c["batches"])
+            combined = {"histories": c["histories"], "batches": c["batches"], "sigma_bar_50pct": csig,
+                        "voxels_above_50pct": cn, "path": "egsgpu_checkpoint on every rank + egsgpu_combine_checkpoints"}
     eff = (1.0 / (sig * sig * T)) if sig else None
 
     # roofline of the dominant kernel: algorithmic bytes / CUDA-event kernel time
@@ -697,7 +717,10 @@ def main():
             "vs_baseline": None, "dtype": "f32" if args.precision == 32 else "f64", "data": "synthetic",
             "config": config_of(wl, H, args.howfarless), "dose_efficiency": eff, "dose_efficiency_unit": "1/(sigma^2 s)",
             "sigma_bar_50pct": sig, "voxels_above_50pct": nsel, "e2e": e2e, "roofline": roof,
-            "gpu_launches": int(launches), "host_seconds": t_host}
+            "gpu_launches": int(launches), "host_seconds": t_host,
+            "autotuner": {"chunk": prof["chunk"], "launch_shape": prof["launch_shape"]}}
+    if combined:
+        line["combined"] = combined
 
     if rank == 0 and args.adjoint:
         line["adjoint"] = adjoint_leg(args, wl, eg, ekw, H)
@@ -736,7 +759,8 @@ def main():
         # the batched configuration (64 phantoms per launch sequence) beside the headline
         b = batched_measure(args, 1, 0, local, None, 3, 3, True, 0.05)
         keep = ("value", "unit", "ms_per_step", "config", "dose_efficiency", "sigma_bar_50pct", "e2e",
-                "one_at_a_time", "fp64_one_at_a_time", "efficiency_ratio_batched_fp32_over_fp64", "gpu_launches")
+                "one_at_a_time", "fp64_one_at_a_time", "efficiency_ratio_batched_fp32_over_fp64", "gpu_launches",
+                "autotuner")
         line["batched64"] = {k: b[k] for k in keep if k in b}
         line["batched64"]["steps"] = 3
     if rank == 0 and ws == 1 and not args.no_cpu:

@@ -35,8 +35,7 @@ class Config(C.Structure):
                 ("ctas_per_sm", C.c_int), ("chunk", C.c_longlong), ("capacity", C.c_longlong),
                 ("requeue_lanes", C.c_int), ("use_graph", C.c_int), ("inter_batch", C.c_int),
                 ("howfarless", C.c_int), ("smax", C.c_double), ("bca_algorithm", C.c_int),
-                ("loop_cap", C.c_int), ("step_cap", C.c_int), ("smem_tables", C.c_int),
-                ("fp64_near_faces", C.c_int)]
+                ("loop_cap", C.c_int), ("step_cap", C.c_int), ("fp64_near_faces", C.c_int)]
 
 
 class SourceStruct(C.Structure):
@@ -477,7 +476,8 @@ class DoseEngine:
         d.update({"launches_" + k: int(o[4 + i]) for i, k in enumerate(keys)})
         d.update(photon_steps=o[8], electron_steps=o[9], photon_pushes=o[10], electron_pushes=o[11],
                  photon_interactions=o[12], electron_interactions=o[13], chunk=int(o[14]),
-                 graph=bool(o[15]), photon_busy_lanes=o[16], electron_busy_lanes=o[17], electron_wide_steps=o[18])
+                 graph=bool(o[15]), photon_busy_lanes=o[16], electron_busy_lanes=o[17], electron_wide_steps=o[18],
+                 launch_shape=int(o[19]))
         return d
 
     def set_history_tally(self, first, n):

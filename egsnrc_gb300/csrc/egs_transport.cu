@@ -103,7 +103,6 @@ struct Params {
     uint32_t seed;
     int requeue_lanes;                    // park survivors of warps this sparse (0 = never)
     int inter_batch;                      // lanes due to interact before the warp samples them
-    int esm_rows;                         // electron PWLF rows staged in shared memory (0 = none)
     int split;                            // FP32 kernels: FP64 near voxel faces and range ends
 };
 
@@ -118,7 +117,6 @@ constexpr int PHOTON_HOPS = 8;
 constexpr int INTER_MAXWAIT = 24;   // longest wait of a lane due to interact
 constexpr int MAX_BLOCK = 128;      // launch bound of the transport kernels (threads per CTA)
 constexpr double VERY_FAR = 1e30;   // egs++ veryFar (egs++/egs_functions.h:105)
-constexpr int SMEM_TABLES_MAX = 96 * 1024;   // largest electron-table staging per CTA (bytes)
 // Distance to a voxel face (cm) within which an FP32 electron step is computed
 // in FP64 when the precision split is on: 2^-12 cm, about 250 FP32 units in
 // the last place of a coordinate of 16 cm.
@@ -1041,24 +1039,7 @@ __device__ __noinline__ Real wide_eloss(const Tables<Real> &T, const MedScalars<
 // carry none of this code.
 template <class Real, bool Multi, bool Adj = false, bool HFL = false, bool PI = false>
 __global__ void __launch_bounds__(MAX_BLOCK, sizeof(Real) == 4 && !Adj ? 6 : 1) k_electron(Params<Real> P) {
-    // The electron PWLF tables of every medium (etab: 16 coefficients per
-    // energy bin, erange: energy and ranges per bin; $SET INTERVAL/$EVALUATE,
-    // src/egsnrc.macros:1226-1262) are staged in shared memory when the launch
-    // gives room for them (P.esm_rows > 0): 16-byte vector copies, then every
-    // bin lookup of the step reads shared memory.
-    extern __shared__ __align__(16) unsigned char e_smem[];
-    Tables<Real> T = P.T;
-    if (P.esm_rows > 0) {
-        Real *se = (Real *)e_smem, *sr = se + (size_t)16 * P.esm_rows;
-        const int4 *ge4 = (const int4 *)P.T.etab, *gr4 = (const int4 *)P.T.erange;
-        int4 *se4 = (int4 *)se, *sr4 = (int4 *)sr;
-        const int ne = 16 * P.esm_rows * (int)sizeof(Real) / 16, nr = 4 * P.esm_rows * (int)sizeof(Real) / 16;
-        for (int i = threadIdx.x; i < ne; i += blockDim.x) se4[i] = ge4[i];
-        for (int i = threadIdx.x; i < nr; i += blockDim.x) sr4[i] = gr4[i];
-        __syncthreads();
-        T.etab = se;
-        T.erange = sr;
-    }
+    const Tables<Real> &T = P.T;
     const Geom<Real> &G = P.G;
     const unsigned lane = threadIdx.x & 31u;
     const unsigned nq = *P.ein.count < P.ein.capacity ? *P.ein.count : P.ein.capacity;
@@ -1928,7 +1909,7 @@ struct Engine : EngineBase {
         out[16] = c[CNT_PITER] ? (double)c[CNT_PLANES] / c[CNT_PITER] : 0.0;
         out[17] = c[CNT_EITER] ? (double)c[CNT_ELANES] / c[CNT_EITER] : 0.0;
         out[18] = (double)c[CNT_EWIDE];
-        out[19] = 0.0;
+        out[19] = (double)shape_sel;
         return 0;
     }
     int history_tally(long long first, long long n, std::string &err) override {
@@ -1978,7 +1959,6 @@ struct Engine : EngineBase {
     int nmed = 0;
     std::vector<MedScalars<Real>> meds;
     DevMem d_etab, d_erange, d_gtab, d_pmax, d_ray, d_rayi, d_shell, d_shellat, d_elem, d_ms, d_msi;
-    int etab_rows = 0;   // electron PWLF bins over all media
     Tables<Real> T{};
     // geometry
     Geom<Real> G{};
@@ -1999,6 +1979,14 @@ struct Engine : EngineBase {
     long long prof_n[4] = {0, 0, 0, 0};
     cudaEvent_t ev[8] = {};
     bool events_ready = false;
+    // Launch-shape candidates: threads per CTA, and resident CTAs per SM of the
+    // photon and electron kernels relative to the most that fit.
+    struct Shape { int bs, dp, de; };
+    static constexpr int NSHAPES = 6;
+    static constexpr Shape SHAPES[NSHAPES] = {{128, 0, 0}, {64, 0, 0}, {96, 0, 0}, {128, 0, -1}, {128, -2, 0},
+                                              {64, 0, -2}};
+    int shape_try = 0, shape_sel = -1;   // next candidate to time; chosen candidate (-1: not yet)
+    double shape_rate[NSHAPES] = {};
     long long tuned_chunk = 0;   // histories per wavefront chosen by the autotuner
     long long best_chunk = 0;
     double best_rate = 0;
@@ -2106,7 +2094,6 @@ struct Engine : EngineBase {
             return cudaMemcpy(d.p, src, bytes, cudaMemcpyHostToDevice);
         };
         CK(up(d_etab, etab.data(), etab.size() * sizeof(Real)));
-        etab_rows = (int)(etab.size() / 16);
         h_etab = etab;
         hatch_ = &H;
         CK(up(d_erange, erange.data(), erange.size() * sizeof(Real)));
@@ -2253,30 +2240,8 @@ struct Engine : EngineBase {
     cudaEvent_t ev_in = nullptr;
     bool graph_ok = true;
 
-    // Shared-memory staging of the electron PWLF tables: the bytes for `rows`
-    // bins of every medium (etab 16 + erange 4 values per bin).
-    static size_t esm_bytes(int rows) { return (size_t)rows * 20 * sizeof(Real); }
-    // Occupancy of an electron kernel and whether its tables are staged in
-    // shared memory: they are when they fit (egsgpu_config.smem_tables != -1)
-    // and staging keeps as many CTAs per SM resident as without it.
-    template <class K>
-    cudaError_t electron_shape(K kern, int bs, int &occ, int &rows) {
-        rows = 0;
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, bs, 0);
-        if (e != cudaSuccess || cfg.smem_tables < 0) return e;
-        const int want = etab_rows;
-        const size_t bytes = esm_bytes(want);
-        if (want <= 0 || bytes > (size_t)SMEM_TABLES_MAX) return cudaSuccess;
-        if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes))) return e;
-        int occ_s = 0;
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, kern, bs, bytes))) return e;
-        if (occ_s >= std::min(occ, cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm : occ)) { rows = want; occ = occ_s; }
-        return cudaSuccess;
-    }
-
     cudaError_t enqueue_rounds(const Params<Real> &P0, int gp, int ge, int bs, bool events, bool multi,
                                bool adj = false, bool hfl = false) {
-        const size_t esm = esm_bytes(P0.esm_rows);
         const bool pi = cfg.bca_algorithm == 1;
         unsigned *counts = (unsigned *)d_counts.p;
         cudaError_t e = cudaSuccess;
@@ -2294,12 +2259,12 @@ struct Engine : EngineBase {
             if ((e = cudaGetLastError())) break;
             if (events && (e = cudaEventRecord(gev[4 * r + 1], ws))) break;
             if (events && (e = cudaEventRecord(gev[4 * r + 2], ws))) break;
-            if (hfl) k_electron<Real, false, false, true><<<ge, bs, esm, ws>>>(P);
-            else if (pi && multi) k_electron<Real, true, false, false, true><<<ge, bs, esm, ws>>>(P);
-            else if (pi) k_electron<Real, false, false, false, true><<<ge, bs, esm, ws>>>(P);
-            else if (adj) k_electron<Real, false, true><<<ge, bs, esm, ws>>>(P);
-            else if (multi) k_electron<Real, true><<<ge, bs, esm, ws>>>(P);
-            else k_electron<Real, false><<<ge, bs, esm, ws>>>(P);
+            if (hfl) k_electron<Real, false, false, true><<<ge, bs, 0, ws>>>(P);
+            else if (pi && multi) k_electron<Real, true, false, false, true><<<ge, bs, 0, ws>>>(P);
+            else if (pi) k_electron<Real, false, false, false, true><<<ge, bs, 0, ws>>>(P);
+            else if (adj) k_electron<Real, false, true><<<ge, bs, 0, ws>>>(P);
+            else if (multi) k_electron<Real, true><<<ge, bs, 0, ws>>>(P);
+            else k_electron<Real, false><<<ge, bs, 0, ws>>>(P);
             if ((e = cudaGetLastError())) break;
             if (events && (e = cudaEventRecord(gev[4 * r + 3], ws))) break;
         }
@@ -2386,11 +2351,9 @@ struct Engine : EngineBase {
             }
             chunk = tuned_chunk;
         }
-        const int bs = cfg.block_size > 0 ? cfg.block_size : 128;
         // persistent grids, one per kernel: never more CTAs than can be
         // resident at once (the photon kernel, with fewer registers, fits more
         // CTAs per SM than the electron kernel)
-        int occ_p = 1, occ_e = 1;
         const bool adj = mode && mode->adj;
         const bool hfl = cfg.howfarless > 0;
         if (hfl && (Multi || mode)) { err = "HOWFARLESS transport is for one homogeneous phantom (no adjoint)"; return EGSGPU_ERR_ARG; }
@@ -2400,24 +2363,44 @@ struct Engine : EngineBase {
             err = "PRESTA-I boundary crossing is for egsgpu_run and egsgpu_run_phantoms (no HOWFARLESS, no adjoint)";
             return EGSGPU_ERR_ARG;
         }
-        int esm_rows = 0;
-        if (hfl) {
+        if (hfl)
             if (int rc = hfl_tables(err)) return rc;
-            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, false, false, true>, bs, 0));
-            CK(electron_shape(k_electron<Real, false, false, true>, bs, occ_e, esm_rows));
-        } else if (pi) {
-            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, Multi>, bs, 0));
-            CK(electron_shape(k_electron<Real, Multi, false, false, true>, bs, occ_e, esm_rows));
-        } else if (adj) {
-            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, false, true>, bs, 0));
-            CK(electron_shape(k_electron<Real, false, true>, bs, occ_e, esm_rows));
-        } else {
-            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, Multi>, bs, 0));
-            CK(electron_shape(k_electron<Real, Multi>, bs, occ_e, esm_rows));
-        }
-        const int cps_cap = cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm : 64;
-        const int gp = sm_count * std::max(1, std::min(cps_cap, occ_p));
-        const int ge = sm_count * std::max(1, std::min(cps_cap, occ_e));
+        // The launch shape of candidate k (see SHAPES): threads per CTA and the
+        // grids of both kernels.
+        int bs = 128, gp = 0, ge = 0;
+        auto shape = [&](int k) -> cudaError_t {
+            const Shape sh = cfg.block_size > 0 || cfg.ctas_per_sm > 0 ? Shape{cfg.block_size > 0 ? cfg.block_size : 128, 0, 0}
+                                                                       : SHAPES[k];
+            bs = sh.bs;
+            int occ_p = 1, occ_e = 1;
+            cudaError_t e;
+            if (hfl) {
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, false, false, true>, bs, 0);
+                if (!e) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, false, false, true>, bs, 0);
+            } else if (pi) {
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, Multi>, bs, 0);
+                if (!e) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, Multi, false, false, true>, bs, 0);
+            } else if (adj) {
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, false, true>, bs, 0);
+                if (!e) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, false, true>, bs, 0);
+            } else {
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, Multi>, bs, 0);
+                if (!e) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, Multi>, bs, 0);
+            }
+            const int cps_cap = cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm : 64;
+            gp = sm_count * std::max(1, std::min(cps_cap, occ_p + sh.dp));
+            ge = sm_count * std::max(1, std::min(cps_cap, occ_e + sh.de));
+            return e;
+        };
+        // Launch-shape autotuner: once the chunk size has settled, successive
+        // chunks of egsgpu_run / egsgpu_run_phantoms try the candidate shapes,
+        // and the fastest (by more than 2% over the first) is kept for the
+        // engine's later runs.  Only without an explicit block_size or
+        // ctas_per_sm, graph replay or adjoint replays; results do not depend
+        // on the shape.
+        const bool tune_shape = cfg.block_size <= 0 && cfg.ctas_per_sm <= 0 && cfg.use_graph <= 0 && !mode;
+        int cur_shape = tune_shape ? (shape_sel >= 0 ? shape_sel : 0) : 0;
+        CK(shape(cur_shape));
         Params<Real> P;
         std::memset(&P, 0, sizeof(P));
         P.T = T; P.G = G;
@@ -2432,7 +2415,6 @@ struct Engine : EngineBase {
         P.seed = seed;
         P.requeue_lanes = cfg.requeue_lanes > 0 ? cfg.requeue_lanes : 0;
         P.inter_batch = cfg.inter_batch > 0 ? std::min(cfg.inter_batch, 32) : (cfg.inter_batch < 0 ? 1 : 8);
-        P.esm_rows = esm_rows;
         P.split = cfg.fp64_near_faces > 0 ? 1 : 0;
         if (Multi) {
             P.probs = (const Geom<Real> *)d_probs.p; P.pseeds = (const uint32_t *)d_pseeds.p;
@@ -2476,6 +2458,11 @@ struct Engine : EngineBase {
             }
             for (long long c0 = b0, cn = 0; c0 < b0 + bn; c0 += cn) {
                 cn = std::min(chunk, b0 + bn - c0);   // the autotuner may change `chunk` below
+                const bool trying = tune_shape && shape_sel < 0 && (!tune || tune_done) && cn == chunk;
+                if (trying && cur_shape != shape_try) {
+                    cur_shape = shape_try;
+                    CK(shape(cur_shape));
+                }
                 auto t_chunk = std::chrono::steady_clock::now();
                 CK(cudaMemsetAsync(counts, 0, 9 * sizeof(unsigned), ws));
                 CK(cudaEventRecord(ev[0], ws));
@@ -2505,6 +2492,20 @@ struct Engine : EngineBase {
                     done = (h[0] == 0 && h[4] == 0);
                 }
                 if (!done) { err = "wavefront did not drain"; return EGSGPU_ERR_LOOP; }
+                if (trying) {
+                    const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_chunk).count();
+                    shape_rate[shape_try] = cn / std::max(dt, 1e-9);
+                    if (++shape_try == NSHAPES) {
+                        int best = 0;
+                        for (int k = 1; k < NSHAPES; ++k)
+                            if (shape_rate[k] > 1.02 * shape_rate[0] && shape_rate[k] > shape_rate[best]) best = k;
+                        shape_sel = best;
+                        if (cur_shape != best) {
+                            cur_shape = best;
+                            CK(shape(cur_shape));
+                        }
+                    }
+                }
                 if (tune && cn == chunk) {
                     double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_chunk).count();
                     double rate = cn / std::max(dt, 1e-9);
@@ -2724,8 +2725,7 @@ struct Engine : EngineBase {
         const int bs = cfg.block_size > 0 ? cfg.block_size : 128;
         int occ_p = 1, occ_e = 1;
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, false>, bs, 0));
-        int esm_rows = 0;
-        CK(electron_shape(k_electron<Real, false>, bs, occ_e, esm_rows));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, false>, bs, 0));
         const int cps_cap = cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm : 64;
         const int gp = sm_count * std::max(1, std::min(cps_cap, occ_p));
         const int ge = sm_count * std::max(1, std::min(cps_cap, occ_e));
@@ -2738,7 +2738,6 @@ struct Engine : EngineBase {
         P.seed = seed;
         P.requeue_lanes = 0;
         P.inter_batch = cfg.inter_batch > 0 ? std::min(cfg.inter_batch, 32) : (cfg.inter_batch < 0 ? 1 : 8);
-        P.esm_rows = esm_rows;
         P.split = cfg.fp64_near_faces > 0 ? 1 : 0;
         // the array keeps the previous call's contents: clear the counters
         CK(cudaMemsetAsync(scratch, 0, 1024, st));
@@ -2756,7 +2755,7 @@ struct Engine : EngineBase {
             P.pin = Q[cur]; P.ein = Q[2 + cur]; P.pout = Q[nxt]; P.eout = Q[2 + nxt];
             k_photon<Real, false><<<gp, bs, 0, st>>>(P);
             CK(cudaGetLastError());
-            k_electron<Real, false><<<ge, bs, esm_bytes(esm_rows), st>>>(P);
+            k_electron<Real, false><<<ge, bs, 0, st>>>(P);
             CK(cudaGetLastError());
             unsigned h[9];
             CK(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, st));

@@ -82,11 +82,6 @@ typedef struct {
                              the run return EGSGPU_ERR_LOOP (the caps are set on
                              the device before each run: handles on one device
                              whose runs overlap share the last caps set) */
-    int smem_tables;      /* electron PWLF tables (every medium's etab and range
-                             rows) staged in shared memory by the electron kernel
-                             when they fit without lowering its occupancy: 0 =
-                             default (staged), -1 = read from global memory
-                             (results are identical either way) */
     int fp64_near_faces;  /* FP32 transport only: 1 computes the electron steps
                              that start within 2^-12 cm of a voxel face or may end
                              the range in FP64 (distances to the faces, residual
@@ -266,7 +261,10 @@ int egsgpu_geometry_query(egsgpu_handle *h, int op, long long n, const int32_t *
  *  photon interactions, electron interactions, autotuned chunk, graph in use,
  *  mean busy lanes per warp iteration in the photon and electron kernels,
  *  electron steps of the FP32 build computed in FP64 near a voxel face or
- *  the end of the range, 0};
+ *  the end of the range, launch shape chosen by the autotuner (-1: none yet;
+ *  0..5 = threads per CTA / resident CTAs per SM of the photon and electron
+ *  kernels relative to the most that fit: 128/0/0, 64/0/0, 96/0/0, 128/0/-1,
+ *  128/-2/0, 64/0/-2)};
  * times are CUDA-event
  * durations on the launch stream.  No counterpart in the reference API
  * (the reference reports CPU time per batch, egs++/egs_timer.cpp). */

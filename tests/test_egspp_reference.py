@@ -145,3 +145,17 @@ def test_fixture_is_the_reference():
         assert EC.digest(where) == FIX["geometry"][name]["where"]
         near = g.hownear(q["near_ireg"], q["near_x"])
         assert EC.digest(near) == FIX["geometry"][name]["hownear"]
+
+
+def test_egspp_application_binding_compiles():
+    # the egs++ application binding against the reference's headers
+    from egsnrc_gb300 import build
+    ref = build.reference_dir()
+    if not ref:
+        pytest.skip("reference sources absent")
+    import subprocess
+    here = os.path.join(os.path.dirname(HERE), "oracle")
+    target = os.path.join("_ref", "egs_gpu_dose_application.o")
+    r = subprocess.run(["make", "-s", target, "REF=" + ref], cwd=here, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert os.path.exists(os.path.join(here, target))

@@ -174,11 +174,9 @@ def test_scheduling_invariance(precision, workload):
     wl = W.WORKLOADS[workload](32)
     n = 40000
     res = []
-    # and the electron tables read from shared or from global memory (the
-    # same values): results must not change
-    for lanes, inter, smem in ((-1, -1, 0), (16, 8, 0), (-1, 24, 0), (-1, -1, -1)):
+    for lanes, inter in ((-1, -1), (16, 8), (-1, 24)):
         eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"], precision=precision, requeue_lanes=lanes,
-                            inter_batch=inter, smem_tables=smem)
+                            inter_batch=inter)
         eng.set_geometry(wl["geometry"])
         eng.set_source(wl["source"])
         eng.set_history_tally(0, n)
@@ -239,3 +237,23 @@ def test_capacity_error_is_reported():
     with pytest.raises(eg.EGSError) as ei:
         eng.run(1000, nbatch=1, seed=1)
     assert ei.value.code == 5
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_launch_shape_autotuner(precision):
+    # a small queue capacity gives many chunks: the chunk size settles, then
+    # successive chunks try every launch shape and the fastest is kept; the
+    # per-history results must equal those of a fixed shape
+    wl = W.slab64(24)
+    n = 400000
+    got = eg.DoseEngine(wl["media"], ecut=wl["ecut"], precision=precision, capacity=1 << 16)
+    ref = eg.DoseEngine(wl["media"], ecut=wl["ecut"], precision=precision, capacity=1 << 16, block_size=128)
+    for e in (got, ref):
+        e.set_geometry(wl["geometry"])
+        e.set_source(wl["source"])
+        e.set_history_tally(0, n)
+        e.run(n, nbatch=1, seed=12)
+    assert 0 <= got.profile()["launch_shape"] < 6
+    assert ref.profile()["launch_shape"] == -1
+    tol = 1e-12 if precision == 64 else 2e-5
+    assert np.allclose(got.history_tally(), ref.history_tally(), rtol=tol, atol=tol)

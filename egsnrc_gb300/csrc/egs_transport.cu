@@ -103,7 +103,6 @@ struct Params {
     uint32_t seed;
     int requeue_lanes;                    // park survivors of warps this sparse (0 = never)
     int inter_batch;                      // lanes due to interact before the warp samples them
-    int split;                            // FP32 kernels: FP64 near voxel faces and range ends
 };
 
 // A warp whose queue is exhausted parks its particles in the next queue once
@@ -1037,7 +1036,9 @@ __device__ __noinline__ Real wide_eloss(const Tables<Real> &T, const MedScalars<
 // ($SET-USTEP), corrected back if howfar cuts it ($SET-TVSTEP), and deflected
 // once at its end by mscat.  Its own instantiation, so that the EXACT kernels
 // carry none of this code.
-template <class Real, bool Multi, bool Adj = false, bool HFL = false, bool PI = false>
+// SPL: the precision split of the FP32 kernel (egsgpu_config.fp64_near_faces),
+// its own instantiation so that the default FP32 step carries none of it.
+template <class Real, bool Multi, bool Adj = false, bool HFL = false, bool PI = false, bool SPL = false>
 __global__ void __launch_bounds__(MAX_BLOCK, sizeof(Real) == 4 && !Adj ? 6 : 1) k_electron(Params<Real> P) {
     const Tables<Real> &T = P.T;
     const Geom<Real> &G = P.G;
@@ -1062,7 +1063,7 @@ __global__ void __launch_bounds__(MAX_BLOCK, sizeof(Real) == 4 && !Adj ? 6 : 1) 
     EList<Real> elstack[Adj ? LSTACK : 1];
     bool alive = false, exhausted = false;
     unsigned long long nstep = 0, npush = 0, ninter = 0, lanes = 0, iters = 0, nwide = 0;
-    constexpr bool SPLIT = sizeof(Real) == 4 && !HFL;   // the FP32 kernels' FP64 steps (`wide`)
+    constexpr bool SPLIT = sizeof(Real) == 4 && !HFL && SPL;   // the FP32 kernel's FP64 steps (`wide`)
     int inter_wait = 0;   // warp-uniform iterations since the first lane became due
     double edep_tot = 0, esc_tot = 0;
     int err = 0;
@@ -1446,7 +1447,7 @@ __global__ void __launch_bounds__(MAX_BLOCK, sizeof(Real) == 4 && !Adj ? 6 : 1) 
             // energy loss are computed in FP64 from the FP32 particle and table
             // values.  Everything else stays FP32; the FP64 build is FP64
             // throughout.
-            const bool wide = SPLIT && P.split && (tperp < (Real)NEAR_FACE || range <= dmin(tstep, tmxs));
+            const bool wide = SPLIT && (tperp < (Real)NEAR_FACE || range <= dmin(tstep, tmxs));
             double range_w = 0;
             if (wide) {
                 tperp = wide_hownear(GP, p.ir, p.x, p.y, p.z);
@@ -1986,6 +1987,7 @@ struct Engine : EngineBase {
     static constexpr Shape SHAPES[NSHAPES] = {{128, 0, 0}, {64, 0, 0}, {96, 0, 0}, {128, 0, -1}, {128, -2, 0},
                                               {64, 0, -2}};
     int shape_try = 0, shape_sel = -1;   // next candidate to time; chosen candidate (-1: not yet)
+    long long shape_cn = 0;              // histories of the chunks the candidates are timed on
     double shape_rate[NSHAPES] = {};
     long long tuned_chunk = 0;   // histories per wavefront chosen by the autotuner
     long long best_chunk = 0;
@@ -2240,6 +2242,28 @@ struct Engine : EngineBase {
     cudaEvent_t ev_in = nullptr;
     bool graph_ok = true;
 
+    // The EXACT electron kernel, or its precision-split instantiation in the
+    // FP32 engine when egsgpu_config.fp64_near_faces is set (PRESTA-I,
+    // HOWFARLESS and the adjoint keep their own kernels).
+    template <bool M>
+    void launch_electron(const Params<Real> &P, int ge, int bs) {
+        if constexpr (sizeof(Real) == 4) {
+            if (cfg.fp64_near_faces > 0) {
+                k_electron<Real, M, false, false, false, true><<<ge, bs, 0, ws>>>(P);
+                return;
+            }
+        }
+        k_electron<Real, M><<<ge, bs, 0, ws>>>(P);
+    }
+    template <bool M>
+    cudaError_t electron_occupancy(int &occ, int bs) {
+        if constexpr (sizeof(Real) == 4) {
+            if (cfg.fp64_near_faces > 0)
+                return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_electron<Real, M, false, false, false, true>, bs, 0);
+        }
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_electron<Real, M>, bs, 0);
+    }
+
     cudaError_t enqueue_rounds(const Params<Real> &P0, int gp, int ge, int bs, bool events, bool multi,
                                bool adj = false, bool hfl = false) {
         const bool pi = cfg.bca_algorithm == 1;
@@ -2263,8 +2287,8 @@ struct Engine : EngineBase {
             else if (pi && multi) k_electron<Real, true, false, false, true><<<ge, bs, 0, ws>>>(P);
             else if (pi) k_electron<Real, false, false, false, true><<<ge, bs, 0, ws>>>(P);
             else if (adj) k_electron<Real, false, true><<<ge, bs, 0, ws>>>(P);
-            else if (multi) k_electron<Real, true><<<ge, bs, 0, ws>>>(P);
-            else k_electron<Real, false><<<ge, bs, 0, ws>>>(P);
+            else if (multi) launch_electron<true>(P, ge, bs);
+            else launch_electron<false>(P, ge, bs);
             if ((e = cudaGetLastError())) break;
             if (events && (e = cudaEventRecord(gev[4 * r + 3], ws))) break;
         }
@@ -2385,7 +2409,7 @@ struct Engine : EngineBase {
                 if (!e) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, false, true>, bs, 0);
             } else {
                 e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, k_photon<Real, Multi>, bs, 0);
-                if (!e) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_electron<Real, Multi>, bs, 0);
+                if (!e) e = electron_occupancy<Multi>(occ_e, bs);
             }
             const int cps_cap = cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm : 64;
             gp = sm_count * std::max(1, std::min(cps_cap, occ_p + sh.dp));
@@ -2415,7 +2439,6 @@ struct Engine : EngineBase {
         P.seed = seed;
         P.requeue_lanes = cfg.requeue_lanes > 0 ? cfg.requeue_lanes : 0;
         P.inter_batch = cfg.inter_batch > 0 ? std::min(cfg.inter_batch, 32) : (cfg.inter_batch < 0 ? 1 : 8);
-        P.split = cfg.fp64_near_faces > 0 ? 1 : 0;
         if (Multi) {
             P.probs = (const Geom<Real> *)d_probs.p; P.pseeds = (const uint32_t *)d_pseeds.p;
             P.psrc = (const Source *)d_psrc.p; P.pvoff = (const int *)d_pvoff.p;
@@ -2458,7 +2481,12 @@ struct Engine : EngineBase {
             }
             for (long long c0 = b0, cn = 0; c0 < b0 + bn; c0 += cn) {
                 cn = std::min(chunk, b0 + bn - c0);   // the autotuner may change `chunk` below
-                const bool trying = tune_shape && shape_sel < 0 && (!tune || tune_done) && cn == chunk;
+                // shapes are timed on chunks of one size: full chunks once the
+                // chunk size has settled, or whole batches smaller than a chunk
+                // (never the remainder of a batch)
+                const bool whole = (cn == chunk && (!tune || tune_done)) || (c0 == b0 && cn == bn && cn < chunk);
+                const bool trying = tune_shape && shape_sel < 0 && whole && (shape_try == 0 || cn == shape_cn);
+                if (trying && shape_try == 0) shape_cn = cn;
                 if (trying && cur_shape != shape_try) {
                     cur_shape = shape_try;
                     CK(shape(cur_shape));
@@ -2738,7 +2766,6 @@ struct Engine : EngineBase {
         P.seed = seed;
         P.requeue_lanes = 0;
         P.inter_batch = cfg.inter_batch > 0 ? std::min(cfg.inter_batch, 32) : (cfg.inter_batch < 0 ? 1 : 8);
-        P.split = cfg.fp64_near_faces > 0 ? 1 : 0;
         // the array keeps the previous call's contents: clear the counters
         CK(cudaMemsetAsync(scratch, 0, 1024, st));
         CK(set_caps(st));
@@ -3425,6 +3452,7 @@ int egsgpu_run_noalloc(egsgpu_handle *h, long long first, long long n, uint32_t 
     if (!h->have_media || !h->have_geom || !h->have_source) { h->err = "media, geometry and source must be set"; return EGSGPU_ERR_STATE; }
     if (h->cfg.bca_algorithm != 0) { h->err = "egsgpu_run_noalloc uses EXACT boundary crossing only"; return EGSGPU_ERR_ARG; }
     if (h->cfg.howfarless > 0) { h->err = "egsgpu_run_noalloc transports voxel by voxel only (no HOWFARLESS)"; return EGSGPU_ERR_ARG; }
+    if (h->cfg.fp64_near_faces > 0) { h->err = "egsgpu_run_noalloc runs the default FP32 step (no fp64_near_faces)"; return EGSGPU_ERR_ARG; }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) { h->err = "no current CUDA device"; return EGSGPU_ERR_CUDA; }
     unsigned char *scratch = nullptr;

@@ -85,8 +85,11 @@ typedef struct {
     int fp64_near_faces;  /* FP32 transport only: 1 computes the electron steps
                              that start within 2^-12 cm of a voxel face or may end
                              the range in FP64 (distances to the faces, residual
-                             range, energy loss); 0 = default (FP32 throughout;
-                             FP64 dose tallies either way) */
+                             range, energy loss), in a kernel of its own; 0 =
+                             default (FP32 throughout; FP64 dose tallies either
+                             way).  For EXACT voxel transport (egsgpu_run,
+                             egsgpu_run_phantoms): PRESTA-I, HOWFARLESS and the
+                             adjoint ignore it, egsgpu_run_noalloc refuses it */
 } egsgpu_config;
 
 /* Source: egs++ EGS_ParallelBeam (sources/egs_parallel_beam) with a point

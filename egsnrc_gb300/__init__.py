@@ -35,7 +35,7 @@ class Config(C.Structure):
                 ("ctas_per_sm", C.c_int), ("chunk", C.c_longlong), ("capacity", C.c_longlong),
                 ("requeue_lanes", C.c_int), ("use_graph", C.c_int), ("inter_batch", C.c_int),
                 ("howfarless", C.c_int), ("smax", C.c_double), ("bca_algorithm", C.c_int),
-                ("loop_cap", C.c_int), ("step_cap", C.c_int), ("ss_batch", C.c_int), ("fp64_near_faces", C.c_int)]
+                ("loop_cap", C.c_int), ("step_cap", C.c_int), ("fp64_near_faces", C.c_int)]
 
 
 class SourceStruct(C.Structure):

@@ -103,7 +103,6 @@ struct Params {
     uint32_t seed;
     int requeue_lanes;                    // park survivors of warps this sparse (0 = never)
     int inter_batch;                      // lanes due to interact before the warp samples them
-    int ss_batch;                         // single-scattering steps due before the warp takes them
 };
 
 // A warp whose queue is exhausted parks its particles in the next queue once
@@ -115,8 +114,6 @@ constexpr int LSTACK = 6;   // per-thread LIFO depth for charged secondaries
 // loop before the warp's bookkeeping (refill, interaction batching) runs again.
 constexpr int PHOTON_HOPS = 8;
 constexpr int INTER_MAXWAIT = 24;   // longest wait of a lane due to interact
-constexpr int SS_MAXWAIT = 24;      // longest wait of a single-scattering step
-constexpr int SS_BATCH_DEFAULT = 12;   // single-scattering steps due before a warp takes them
 constexpr int MAX_BLOCK = 128;      // launch bound of the transport kernels (threads per CTA)
 constexpr double VERY_FAR = 1e30;   // egs++ veryFar (egs++/egs_functions.h:105)
 // Distance to a voxel face (cm) within which an FP32 electron step is computed
@@ -1068,8 +1065,6 @@ __global__ void __launch_bounds__(MAX_BLOCK, sizeof(Real) == 4 && !Adj ? 6 : 1) 
     unsigned long long nstep = 0, npush = 0, ninter = 0, lanes = 0, iters = 0, nwide = 0;
     constexpr bool SPLIT = sizeof(Real) == 4 && !HFL && SPL;   // the FP32 kernel's FP64 steps (`wide`)
     int inter_wait = 0;   // warp-uniform iterations since the first lane became due
-    int ss_wait = 0;      // warp-uniform iterations since single-scattering steps became due
-    constexpr bool SSB = !HFL && !PI;   // single-scattering batching (EXACT boundary crossing)
     double edep_tot = 0, esc_tot = 0;
     int err = 0;
     const Real rm = (Real)RM;
@@ -1148,31 +1143,6 @@ __global__ void __launch_bounds__(MAX_BLOCK, sizeof(Real) == 4 && !Adj ? 6 : 1) 
         if (!live) break;
         lanes += __popc(live);
         ++iters;
-        // Single-scattering batching (EXACT boundary crossing): a step that
-        // starts within the skin depth of a voxel face takes the single-
-        // scattering path of the step below, any other the PRESTA-II path.
-        // Such steps wait until enough of the warp's condensed-history steps
-        // are due one (or SS_MAXWAIT iterations), so that the warp runs each
-        // of the two long paths with more lanes.  A waiting lane only skips
-        // iterations: its random numbers and results do not change.
-        bool ss_hold = false;
-        if (SSB) {
-            bool near = false;
-            if (alive && s.state == 2) {
-                const MedScalars<Real> &M = cmed<Real>(s.medium);
-                const Geom<Real> &GP = geom_of<Real, Multi>(P, p.pb);
-                const Real tperp = hownear(GP, p.ir, p.x, p.y, p.z);
-                const Real p2 = s.eke * (s.eke + 2 * rm), beta2 = p2 / (p2 + rm * rm);
-                near = tperp < T.skindepth * (beta2 / (s.rhor * M.blcc));
-            }
-            const unsigned nm = __ballot_sync(0xffffffffu, near);
-            if (nm && P.ss_batch > 1) {
-                const int n2 = __popc(__ballot_sync(0xffffffffu, alive && s.state == 2));
-                ++ss_wait;
-                if (__popc(nm) >= min(P.ss_batch, n2) || ss_wait > SS_MAXWAIT) ss_wait = 0;
-                else ss_hold = near;
-            }
-        }
         // Discrete interactions are sampled for several lanes at once (see the
         // photon kernel).
         {
@@ -1404,7 +1374,7 @@ __global__ void __launch_bounds__(MAX_BLOCK, sizeof(Real) == 4 && !Adj ? 6 : 1) 
                 continue;
             }
         }
-        if (!alive || s.state == 3 || ss_hold) continue;
+        if (!alive || s.state == 3) continue;
 
         const int qel = (1 + p.iq) / 2;
         bool ecut_discard = false;
@@ -2469,7 +2439,6 @@ struct Engine : EngineBase {
         P.seed = seed;
         P.requeue_lanes = cfg.requeue_lanes > 0 ? cfg.requeue_lanes : 0;
         P.inter_batch = cfg.inter_batch > 0 ? std::min(cfg.inter_batch, 32) : (cfg.inter_batch < 0 ? 1 : 8);
-        P.ss_batch = cfg.ss_batch > 0 ? std::min(cfg.ss_batch, 32) : (cfg.ss_batch < 0 ? 1 : SS_BATCH_DEFAULT);
         if (Multi) {
             P.probs = (const Geom<Real> *)d_probs.p; P.pseeds = (const uint32_t *)d_pseeds.p;
             P.psrc = (const Source *)d_psrc.p; P.pvoff = (const int *)d_pvoff.p;
@@ -2797,7 +2766,6 @@ struct Engine : EngineBase {
         P.seed = seed;
         P.requeue_lanes = 0;
         P.inter_batch = cfg.inter_batch > 0 ? std::min(cfg.inter_batch, 32) : (cfg.inter_batch < 0 ? 1 : 8);
-        P.ss_batch = cfg.ss_batch > 0 ? std::min(cfg.ss_batch, 32) : (cfg.ss_batch < 0 ? 1 : SS_BATCH_DEFAULT);
         // the array keeps the previous call's contents: clear the counters
         CK(cudaMemsetAsync(scratch, 0, 1024, st));
         CK(set_caps(st));

@@ -82,11 +82,6 @@ typedef struct {
                              the run return EGSGPU_ERR_LOOP (the caps are set on
                              the device before each run: handles on one device
                              whose runs overlap share the last caps set) */
-    int ss_batch;         /* condensed-history steps of a warp due to take the
-                             single-scattering path (within the skin depth of a
-                             face) before the warp takes them together; 0 =
-                             default (12), -1 = immediately (results are
-                             identical either way) */
     int fp64_near_faces;  /* FP32 transport only: 1 computes the electron steps
                              that start within 2^-12 cm of a voxel face or may end
                              the range in FP64 (distances to the faces, residual

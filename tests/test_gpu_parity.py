@@ -174,10 +174,9 @@ def test_scheduling_invariance(precision, workload):
     wl = W.WORKLOADS[workload](32)
     n = 40000
     res = []
-    # and so does holding single-scattering steps for a batch
-    for lanes, inter, ssb in ((-1, -1, -1), (16, 8, 12), (-1, 24, 24), (-1, 8, 4)):
+    for lanes, inter in ((-1, -1), (16, 8), (-1, 24)):
         eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"], precision=precision, requeue_lanes=lanes,
-                            inter_batch=inter, ss_batch=ssb)
+                            inter_batch=inter)
         eng.set_geometry(wl["geometry"])
         eng.set_source(wl["source"])
         eng.set_history_tally(0, n)

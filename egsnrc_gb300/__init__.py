@@ -476,7 +476,7 @@ class DoseEngine:
         d.update({"launches_" + k: int(o[4 + i]) for i, k in enumerate(keys)})
         d.update(photon_steps=o[8], electron_steps=o[9], photon_pushes=o[10], electron_pushes=o[11],
                  photon_interactions=o[12], electron_interactions=o[13], chunk=int(o[14]),
-                 graph=bool(o[15]), photon_busy_lanes=o[16], electron_busy_lanes=o[17], electron_wide_steps=o[18],
+                 graph=int(o[15]), photon_busy_lanes=o[16], electron_busy_lanes=o[17], electron_wide_steps=o[18],
                  launch_shape=int(o[19]))
         return d
 

@@ -1671,6 +1671,22 @@ __global__ void k_batch(double *d, double *sum, double *sum2, long long n) {
     }
 }
 
+// Loop control of the device-side wavefront loop (egsgpu_config.use_graph = 2):
+// runs after each pair of rounds inside a conditional WHILE graph node and
+// keeps the loop going while either next input queue (photon queue 0, count
+// counts[0]; electron queue 2, count counts[4]) holds particles, for at most
+// `limit` rounds; a loop stopped by the limit sets the loop-cap error flag.
+__global__ void k_rounds(cudaGraphConditionalHandle hc, const unsigned *counts, unsigned *rounds, unsigned limit,
+                         int *error) {
+    const unsigned r = (rounds[0] += 2);
+    bool more = counts[0] != 0 || counts[4] != 0;
+    if (more && r >= limit) {
+        error[1] = 1;
+        more = false;
+    }
+    cudaGraphSetConditional(hc, more ? 1u : 0u);
+}
+
 // Geometry queries on one phantom through the transport kernels' own
 // functions (a checking aid): op 0 isWhere of x; op 1 howfar from region
 // ireg (howfarFromOut when ireg < 0) along u within t, writing the new region
@@ -1906,7 +1922,7 @@ struct Engine : EngineBase {
         out[10] = (double)c[CNT_PUSH]; out[11] = (double)c[CNT_EPUSH];
         out[12] = (double)c[CNT_INTER]; out[13] = (double)c[CNT_EINTER];
         out[14] = (double)tuned_chunk;
-        out[15] = gexec ? 1.0 : 0.0;
+        out[15] = gexec_loop ? 2.0 : (gexec ? 1.0 : 0.0);
         out[16] = c[CNT_PITER] ? (double)c[CNT_PLANES] / c[CNT_PITER] : 0.0;
         out[17] = c[CNT_EITER] ? (double)c[CNT_ELANES] / c[CNT_EITER] : 0.0;
         out[18] = (double)c[CNT_EWIDE];
@@ -2001,6 +2017,7 @@ struct Engine : EngineBase {
     }
     ~Engine() {
         if (gexec) cudaGraphExecDestroy(gexec);
+        if (gexec_loop) cudaGraphExecDestroy(gexec_loop);
         if (events_ready) {
             for (auto &e : ev) cudaEventDestroy(e);
             for (auto &e : gev) cudaEventDestroy(e);
@@ -2265,11 +2282,11 @@ struct Engine : EngineBase {
     }
 
     cudaError_t enqueue_rounds(const Params<Real> &P0, int gp, int ge, int bs, bool events, bool multi,
-                               bool adj = false, bool hfl = false) {
+                               bool adj = false, bool hfl = false, int nrounds = ROUNDS) {
         const bool pi = cfg.bca_algorithm == 1;
         unsigned *counts = (unsigned *)d_counts.p;
         cudaError_t e = cudaSuccess;
-        for (int r = 0; r < ROUNDS && e == cudaSuccess; ++r) {
+        for (int r = 0; r < nrounds && e == cudaSuccess; ++r) {
             int cur = r & 1, nxt = 1 - cur;
             Params<Real> P = P0;
             P.pin = q[cur]; P.ein = q[2 + cur]; P.pout = q[nxt]; P.eout = q[2 + nxt];
@@ -2314,6 +2331,58 @@ struct Engine : EngineBase {
             cudaGetLastError();
             if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
             graph_ok = false;
+        }
+    }
+
+    // Device-side wavefront loop (egsgpu_config.use_graph = 2): a graph whose
+    // conditional WHILE node repeats a body of two rounds (queues 0 -> 1 -> 0)
+    // and k_rounds, so that one graph launch per chunk transports it to the
+    // end without the host looking at the queues in between.  On any failure
+    // the engine falls back to launching the rounds directly.
+    static constexpr unsigned MAX_ROUNDS = 100000;
+    cudaGraphExec_t gexec_loop = nullptr;
+    bool loop_ok = true;
+    DevMem d_rounds;
+
+    void build_loop_graph(const Params<Real> &P0, int gp, int ge, int bs, bool multi, bool hfl) {
+        if (gexec_loop) { cudaGraphExecDestroy(gexec_loop); gexec_loop = nullptr; }
+        cudaGraph_t g = nullptr;
+        cudaError_t e = d_rounds.alloc(sizeof(unsigned));
+        if (e == cudaSuccess) e = cudaGraphCreate(&g, 0);
+        cudaGraphConditionalHandle hc = 0;
+        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hc, g, 1, cudaGraphCondAssignDefault);
+        // (the parameter union has no default constructor: zeroed storage)
+        alignas(cudaGraphNodeParams) unsigned char np_raw[sizeof(cudaGraphNodeParams)] = {};
+        cudaGraphNodeParams &np = *reinterpret_cast<cudaGraphNodeParams *>(np_raw);
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = hc;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node = nullptr;
+        if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+        bool capturing = false;
+        if (e == cudaSuccess) {
+            e = cudaStreamBeginCaptureToGraph(ws, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal);
+            capturing = e == cudaSuccess;
+        }
+        if (e == cudaSuccess) e = enqueue_rounds(P0, gp, ge, bs, false, multi, false, hfl, 2);
+        if (e == cudaSuccess) {
+            k_rounds<<<1, 1, 0, ws>>>(hc, (const unsigned *)d_counts.p, (unsigned *)d_rounds.p, MAX_ROUNDS,
+                                      (int *)d_error.p);
+            e = cudaGetLastError();
+        }
+        if (capturing) {
+            cudaGraph_t body = nullptr;
+            cudaError_t e2 = cudaStreamEndCapture(ws, &body);
+            if (e == cudaSuccess) e = e2;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&gexec_loop, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            if (gexec_loop) { cudaGraphExecDestroy(gexec_loop); gexec_loop = nullptr; }
+            loop_ok = false;
         }
     }
 
@@ -2452,9 +2521,12 @@ struct Engine : EngineBase {
             P.requeue_lanes = 0;
         }
         P.pin = q[0]; P.ein = q[2]; P.pout = q[0]; P.eout = q[2];
-        const bool use_graph = cfg.use_graph > 0 && graph_ok && !mode;
+        const bool use_graph = cfg.use_graph == 1 && graph_ok && !mode;
         if (use_graph) build_graph(P, gp, ge, bs, Multi, hfl);
         const bool graph = use_graph && gexec;
+        const bool use_loop = cfg.use_graph == 2 && loop_ok && !mode;
+        if (use_loop) build_loop_graph(P, gp, ge, bs, Multi, hfl);
+        const bool looping = use_loop && gexec_loop;
         unsigned *counts = (unsigned *)d_counts.p;
         CK(cudaEventRecord(ev_in, st));
         CK(cudaStreamWaitEvent(ws, ev_in, 0));
@@ -2499,7 +2571,22 @@ struct Engine : EngineBase {
                 CK(cudaEventRecord(ev[1], ws));
                 unsigned h[9] = {};
                 bool done = false;
-                for (int rep = 0; rep < 100000 / ROUNDS && !done; ++rep) {
+                if (looping) {   // one launch runs the chunk's rounds on the device
+                    unsigned nr = 0;
+                    CK(cudaMemsetAsync(d_rounds.p, 0, sizeof(unsigned), ws));
+                    CK(cudaGraphLaunch(gexec_loop, ws));
+                    CK(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, ws));
+                    CK(cudaMemcpyAsync(&nr, d_rounds.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ws));
+                    CK(cudaStreamSynchronize(ws));
+                    prof_ms[0] += elapsed(ev[0], ev[1]); ++prof_n[0];
+                    prof_n[1] += nr; prof_n[2] += nr;
+                    if (h[8] > capacity || h[0] > capacity || h[4] > capacity) {
+                        err = "particle queue capacity exceeded; lower egsgpu_config.chunk or raise capacity";
+                        return EGSGPU_ERR_CAPACITY;
+                    }
+                    done = (h[0] == 0 && h[4] == 0);
+                }
+                for (int rep = 0; rep < 100000 / ROUNDS && !done && !looping; ++rep) {
                     if (graph) CK(cudaGraphLaunch(gexec, ws));
                     else CK(enqueue_rounds(P, gp, ge, bs, true, Multi, adj, hfl));
                     CK(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, ws));

@@ -49,8 +49,13 @@ typedef struct {
     int requeue_lanes;    /* a warp whose queue is empty parks its particles for the
                              next round once this few lanes are busy; <= 0 = never
                              (default; results are identical either way) */
-    int use_graph;        /* 1: replay the wavefront rounds from a CUDA graph (no
-                             per-kernel timing); 0: direct launches with CUDA events */
+    int use_graph;        /* 1: replay the wavefront rounds from a CUDA graph, four
+                             rounds per host check of the queues; 2: one graph
+                             launch per chunk whose conditional WHILE node repeats
+                             the rounds on the device until the queues drain (no
+                             host round trips inside a chunk); 0: direct launches
+                             with CUDA events around every kernel.  Graphs give
+                             no per-kernel timing; results are identical */
     int inter_batch;      /* lanes of a warp due to interact before their interactions
                              are sampled together; 0 = default (8), -1 = immediately
                              (results are identical either way) */
@@ -261,7 +266,8 @@ int egsgpu_geometry_query(egsgpu_handle *h, int op, long long n, const int32_t *
 /* Device-side profile of the runs since the last reset: out[20] =
  * {ms source, ms photon, ms electron, ms batch, launches of each (4),
  *  photon steps, electron steps, photon-kernel pushes, electron-kernel pushes,
- *  photon interactions, electron interactions, autotuned chunk, graph in use,
+ *  photon interactions, electron interactions, autotuned chunk, graph in use
+ *  (0 none, 1 round replay, 2 device-side loop),
  *  mean busy lanes per warp iteration in the photon and electron kernels,
  *  electron steps of the FP32 build computed in FP64 near a voxel face or
  *  the end of the range, launch shape chosen by the autotuner (-1: none yet;

@@ -135,3 +135,29 @@ def test_adjoint_full_physics_photon_beam_known_gap():
     ratio = u / f
     print("\nphoton beam, uniform scaling: adjoint %.4g +- %.2g, FD %.4g +- %.2g, ratio %.3f" % (u, su, f, sf, ratio))
     assert 0.4 < ratio < 0.85, ratio
+
+
+def test_adjoint_against_brute_force_resimulation():
+    # the reference gradient by brute force: independent re-simulations (no
+    # common random numbers) at densities scaled by 1 +- h, many histories each;
+    # the seed-replay adjoint of the electron beam must agree with it within
+    # its statistical error and 5%
+    g, src = full_physics_case(-1)
+    eng = eg.DoseEngine([W.WATER], ecut=0.521, pcut=0.01, precision=32)
+    eng.set_source(src)
+    n, h, M = 400000, 0.05, 6
+    ones = np.ones(g.nvox)
+    adj = []
+    for m in range(2):
+        dose(eng, g, g.rhor, n, 500 + m)
+        adj.append(float(g.rhor @ eng.adjoint(ones, n, seed=500 + m)))
+    bf = []
+    for m in range(M):
+        lp = dose(eng, g, g.rhor * (1 + h), n, 600 + 2 * m).sum()
+        lm = dose(eng, g, g.rhor * (1 - h), n, 601 + 2 * m).sum()
+        bf.append((lp - lm) / (2 * h))
+    eng.close()
+    a, b = np.mean(adj), np.mean(bf)
+    sb = np.std(bf, ddof=1) / np.sqrt(M)
+    print("\nelectron beam, uniform scaling: adjoint %.4g, brute-force re-simulation %.4g +- %.2g" % (a, b, sb))
+    assert abs(a - b) < 3 * sb + 0.05 * abs(a), (a, b, sb)

@@ -271,7 +271,7 @@ def reference_arm(args, wl, ws, rank, dist):
     line = {"impl": "reference", "metric": "histories_per_second", "value": value, "unit": "histories/s",
             "n_gpus": args.gpus, "steps": K, "warmup": W, "ms_per_step": 1e3 * T / K,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": config_of(wl, per_step),
+            "data": "synthetic", "config": config_of(wl), "histories_per_step": int(per_step),
             "dose_efficiency": eff, "sigma_bar_50pct": sig,
             "cpu_baseline": {"value": value, "unit": "histories/s", "cores": threads, "kind": "port",
                              "sample": "%d histories per step x %d steps of %s (FP64 CPU restatement of the "
@@ -281,11 +281,14 @@ def reference_arm(args, wl, ws, rank, dist):
     print(json.dumps(line), flush=True)
 
 
-def config_of(wl, per_step, howfarless=False):
+def config_of(wl, howfarless=False):
+    """The workload: the same dict for both arms.  How many histories one
+    step transports is a measurement parameter, reported beside it
+    (`histories_per_step`): the rate is per history."""
     g = wl["geometry"]
     return {"workload": wl["name"] + ("-howfarless" if howfarless else ""),
             "phantom": "%dx%dx%d voxels" % (g.nx, g.ny, g.nz),
-            "media": wl["media"], "histories_per_step": int(per_step), "batches_per_step": 1,
+            "media": wl["media"], "batches_per_step": 1,
             "ecut_MeV": wl["ecut"], "pcut_MeV": wl["pcut"],
             "l2": "256 MiB buffer written between timed steps"}
 
@@ -718,7 +721,8 @@ def main():
     line = {"metric": "histories_per_second", "value": value, "unit": "histories/s", "n_gpus": ws, "steps": K,
             "warmup": Wm, "ms_per_step": 1e3 * T / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32" if args.precision == 32 else "f64", "data": "synthetic",
-            "config": config_of(wl, H, args.howfarless), "dose_efficiency": eff, "dose_efficiency_unit": "1/(sigma^2 s)",
+            "config": config_of(wl, args.howfarless), "histories_per_step": int(H), "dose_efficiency": eff,
+            "dose_efficiency_unit": "1/(sigma^2 s)",
             "sigma_bar_50pct": sig, "voxels_above_50pct": nsel, "e2e": e2e, "roofline": roof,
             "gpu_launches": int(launches), "host_seconds": t_host,
             "autotuner": {"chunk": prof["chunk"], "launch_shape": prof["launch_shape"]}}

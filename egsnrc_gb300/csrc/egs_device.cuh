@@ -157,12 +157,39 @@ __host__ __device__ inline uint64_t child_sid(uint64_t sid, uint32_t n, uint32_t
 // (internal linkage: each translation unit of the engine has its own copy)
 static __device__ __noinline__ uint4 philox_block(uint32_t b, uint32_t s0, uint32_t s1, uint32_t k0, uint32_t k1);
 
+// The generator keeps a window of the stream's next four Philox blocks
+// (block b in slot b & 3; `next` is one past the highest block held).  A
+// draw refills only when its block is missing.  The transport loops call
+// ahead(k) where the warp is converged, so that the blocks the lanes will
+// need for the coming step are computed there, by all lanes together, instead
+// of at whichever draw site a lane's counter happens to cross into a new block
+// (the lanes' counters are out of phase, so in a lazily filled stream almost
+// every draw site runs the ten Philox rounds for one or two of its lanes).
+// The numbers are the same either way: the window only decides when a block
+// is computed.  A copy holds the stream position but not the window, so
+// particle copies stay small and a copy never reads blocks it did not compute.
 struct Rng {
-    uint32_t seed, hist, n, blk;
+    uint32_t seed, hist, n, next;
     uint64_t sid;
-    uint32_t c0, c1, c2, c3;
+    alignas(16) uint32_t c[16];
+    Rng() = default;
+    __host__ __device__ Rng(const Rng &o) : seed(o.seed), hist(o.hist), n(o.n), next(0), sid(o.sid) {}
+    __host__ __device__ Rng &operator=(const Rng &o) {
+        seed = o.seed; hist = o.hist; n = o.n; sid = o.sid; next = 0;
+        return *this;
+    }
     __device__ void init(uint32_t s, uint32_t h, uint64_t id, uint32_t n0) {
-        seed = s; hist = h; sid = id; n = n0; blk = 0xffffffffu;
+        seed = s; hist = h; sid = id; n = n0; next = 0;
+    }
+    __device__ inline void fill(uint32_t b) {
+        reinterpret_cast<uint4 *>(c)[b & 3u] = philox_block(b, (uint32_t)sid, (uint32_t)(sid >> 32), seed, hist);
+    }
+    // make the blocks holding the next k numbers (k <= 13) present
+    __device__ inline void ahead(uint32_t k) {
+        const uint32_t b0 = n >> 2, b1 = (n + k - 1) >> 2;
+        uint32_t b = next > b0 ? next : b0;
+        for (; b <= b1; ++b) fill(b);
+        if (b > next) next = b;
     }
     // Out of line (as is azimuth): the electron step loop is larger than the
     // instruction caches, and one shared copy of the draw for its ~30 call
@@ -176,13 +203,11 @@ struct Rng {
         return make_float2(a, draw());
     }
     __device__ inline float draw() {
-        uint32_t b = n >> 2;
-        if (b != blk) {
-            uint4 o = philox_block(b, (uint32_t)sid, (uint32_t)(sid >> 32), seed, hist);
-            c0 = o.x; c1 = o.y; c2 = o.z; c3 = o.w;
-            blk = b;
-        }
-        uint32_t j = n & 3u, x = (j == 0) ? c0 : (j == 1) ? c1 : (j == 2) ? c2 : c3;
+        const uint32_t b = n >> 2;
+        // present: b < next, and b >= next - 4 since ahead() never runs more
+        // than three blocks past the current one
+        if (b >= next) { fill(b); next = b + 1; }
+        const uint32_t x = c[n & 15u];
         ++n;
         // (x >> 9) + 0.5 scaled by 2^-23: exact in FP32 and FP64, in (0,1)
         return ((float)(x >> 9) + 0.5f) * (1.0f / 8388608.0f);

@@ -114,6 +114,11 @@ constexpr int LSTACK = 6;   // per-thread LIFO depth for charged secondaries
 // loop before the warp's bookkeeping (refill, interaction batching) runs again.
 constexpr int PHOTON_HOPS = 8;
 constexpr int INTER_MAXWAIT = 24;   // longest wait of a lane due to interact
+// Random numbers made present ahead of an electron step or an interaction
+// batch: a PRESTA-II step with the q-surface sampler takes 11 (two
+// deflections, two azimuths, the lateral displacement), plus one for a new
+// step length and one for the fictitious-cross-section test.
+constexpr unsigned RNG_AHEAD = 13;
 constexpr int MAX_BLOCK = 128;      // launch bound of the transport kernels (threads per CTA)
 constexpr double VERY_FAR = 1e30;   // egs++ veryFar (egs++/egs_functions.h:105)
 // Distance to a voxel face (cm) within which an FP32 electron step is computed
@@ -757,6 +762,7 @@ __global__ void __launch_bounds__(MAX_BLOCK, sizeof(Real) == 4 ? 8 : 1) k_photon
                 inter_wait = 0;
                 if (alive && s.state == 3) {
                 // interaction
+                p.rng.ahead(RNG_AHEAD);   // the batch's blocks, computed together
                 ++ninter;
                 if (Adj) gadd(P, ga, p.ir, Gh / s.rhor);
                 const MedScalars<Real> &M = cmed<Real>(s.medium);
@@ -1143,6 +1149,9 @@ __global__ void __launch_bounds__(MAX_BLOCK, sizeof(Real) == 4 && !Adj ? 6 : 1) 
         if (!live) break;
         lanes += __popc(live);
         ++iters;
+        // the random-number blocks of the coming step, computed by the warp's
+        // live lanes together (Rng::ahead)
+        if (alive) p.rng.ahead(RNG_AHEAD);
         // Discrete interactions are sampled for several lanes at once (see the
         // photon kernel).
         {

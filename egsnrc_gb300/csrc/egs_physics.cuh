@@ -445,7 +445,10 @@ __device__ inline void mscat(const Tables<Real> &T, Rng &r, Real lambda, Real ch
             Real ai = llmbda * T.dllambi;
             int i = (int)ai;
             ai -= i;
-            Real xi = urand<Real>(r);
+            const bool drawj = !(q1 < (Real)1e-3) && q1 < (Real)0.5;
+            float2 qij;
+            if (drawj) qij = urand2(r); else qij = make_float2(r.u(), 0.f);
+            Real xi = (Real)qij.x;
             if (xi < ai) ++i;
             i = min(max(i, 0), MS_NL - 1);
             int j;
@@ -454,7 +457,7 @@ __device__ inline void mscat(const Tables<Real> &T, Rng &r, Real lambda, Real ch
                 Real aj = q1 * T.dqmsi;
                 j = (int)aj;
                 aj -= j;
-                xi = urand<Real>(r);
+                xi = (Real)qij.y;
                 if (xi < aj) ++j;
             } else j = MS_NQ - 1;
             Real om;
@@ -466,7 +469,8 @@ __device__ inline void mscat(const Tables<Real> &T, Rng &r, Real lambda, Real ch
             st.i = i; st.j = j;
             st.find_index = false;
         }
-        Real xi = urand<Real>(r);
+        const float2 qku = urand2(r);
+        Real xi = (Real)qku.x;
         Real ak = xi * (MS_NU - 1);
         int k = (int)ak;
         ak -= k;
@@ -474,7 +478,7 @@ __device__ inline void mscat(const Tables<Real> &T, Rng &r, Real lambda, Real ch
         if (ak > T.ms[(base + k) * 3 + 2]) k = T.ms_i[base + k];
         k = min(max(k, 0), MS_NU - 2);
         Real a = T.ms[(base + k) * 3 + 1], u = T.ms[(base + k) * 3], du = T.ms[(base + k + 1) * 3] - u;
-        xi = urand<Real>(r);
+        xi = (Real)qku.y;
         if (dabs(a) < (Real)0.2) {
             Real x1 = (Real)0.5 * (1 - xi) * a;
             u = u + xi * du * (1 + x1 * (1 - xi * a));

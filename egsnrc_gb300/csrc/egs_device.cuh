@@ -184,11 +184,17 @@ struct Rng {
     __device__ inline void fill(uint32_t b) {
         reinterpret_cast<uint4 *>(c)[b & 3u] = philox_block(b, (uint32_t)sid, (uint32_t)(sid >> 32), seed, hist);
     }
-    // make the blocks holding the next k numbers (k <= 13) present
+    // make the blocks holding the next k numbers (k <= 13) present.  The ten
+    // rounds are inlined here (one copy per transport loop): a call to the
+    // shared out-of-line block from this site measured 10-20% slower.
     __device__ inline void ahead(uint32_t k) {
         const uint32_t b0 = n >> 2, b1 = (n + k - 1) >> 2;
         uint32_t b = next > b0 ? next : b0;
-        for (; b <= b1; ++b) fill(b);
+        for (; b <= b1; ++b) {
+            uint32_t o[4];
+            philox10(b, (uint32_t)sid, (uint32_t)(sid >> 32), 0u, seed, hist, o);
+            reinterpret_cast<uint4 *>(c)[b & 3u] = make_uint4(o[0], o[1], o[2], o[3]);
+        }
         if (b > next) next = b;
     }
     // Out of line (as is azimuth): the electron step loop is larger than the

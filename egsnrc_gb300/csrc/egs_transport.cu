@@ -2225,10 +2225,26 @@ struct Engine : EngineBase {
         return 0;
     }
 
+    static constexpr size_t QUEUE_RECORD = 12 * sizeof(Real) + sizeof(int) + 2 * sizeof(int8_t) +
+                                           2 * sizeof(uint32_t) + sizeof(unsigned long long);
+    // Records per queue when egsgpu_config.capacity is 0: the largest power of
+    // two from 2^27 down to 2^20 whose four queues take at most a sixth of the
+    // device memory free when the handle first runs (2^27 on a GB300 with
+    // nothing else resident: 37.6 GB in FP32).  Larger queues let the chunk
+    // autotuner run more histories per wavefront, and each chunk ends in a few
+    // short, sparsely occupied rounds: slab64 runs 6% faster at 2^27 than at
+    // 2^25.  Results do not depend on the capacity.
+    unsigned default_capacity() {
+        if (capacity > 0) return capacity;
+        size_t fr = 0, tot = 0;
+        if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { cudaGetLastError(); return 1u << 25; }
+        for (int b = 27; b > 20; --b)
+            if (4 * (((size_t)1 << b) * QUEUE_RECORD + 1024) <= fr / 6) return 1u << b;
+        return 1u << 20;
+    }
     int ensure_queues(unsigned cap, std::string &err) {
         if (cap <= capacity) return 0;
-        size_t per = 12 * sizeof(Real) + sizeof(int) + 2 * sizeof(int8_t) + 2 * sizeof(uint32_t) +
-                     sizeof(unsigned long long);
+        const size_t per = QUEUE_RECORD;
         CK(d_counts.alloc(16 * sizeof(unsigned)));
         for (int k = 0; k < 4; ++k) {
             CK(qmem[k].alloc((size_t)cap * per + 1024));
@@ -2429,7 +2445,7 @@ struct Engine : EngineBase {
     int run_impl(const Source &S, long long first, long long n, int nbatch, uint32_t seed, cudaStream_t st,
                  std::string &err) {
         if (!G.xb) { err = "geometry not set"; return EGSGPU_ERR_STATE; }
-        unsigned cap = cfg.capacity > 0 ? (unsigned)std::min<long long>(cfg.capacity, 0x7fffffffLL) : (1u << 25);
+        unsigned cap = cfg.capacity > 0 ? (unsigned)std::min<long long>(cfg.capacity, 0x7fffffffLL) : default_capacity();
         if (int rc = ensure_queues(cap, err)) return rc;
         if (!events_ready) {
             for (auto &e : ev) CK(cudaEventCreate(&e));

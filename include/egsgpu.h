@@ -45,7 +45,8 @@ typedef struct {
     int block_size;       /* threads per CTA for the transport kernels; 0 = default */
     int ctas_per_sm;      /* resident CTAs per SM; 0 = default                       */
     long long chunk;      /* histories per wavefront chunk; 0 = automatic   */
-    long long capacity;   /* particle-queue capacity per queue; 0 = automatic */
+    long long capacity;   /* particle-queue capacity per queue; 0 = automatic: the largest power of two
+                             up to 2^27 whose four queues fit in a sixth of the free device memory */
     int requeue_lanes;    /* a warp whose queue is empty parks its particles for the
                              next round once this few lanes are busy; <= 0 = never
                              (default; results are identical either way) */

@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--graph", type=int, default=0, choices=[0, 1, 2],
                     help="wavefront rounds: 0 direct launches, 1 graph replay, 2 device-side loop per chunk")
     ap.add_argument("--ctas-per-sm", type=int, default=0, help="resident CTAs per SM (0 = as many as fit)")
+    ap.add_argument("--inter-batch", type=int, default=0,
+                    help="lanes a warp gathers before it samples their interactions together (0 = engine default)")
     ap.add_argument("--clock-period", type=float, default=0.2, help="seconds between clock samples")
     ap.add_argument("--clock-mode", default="nvml", choices=["nvml", "process", "off"])
     ap.add_argument("--adjoint", action="store_true",
@@ -380,7 +382,7 @@ def batched_measure(args, ws, rank, local, dist, K, Wm, no_cpu, fp64_frac):
     import egsnrc_gb300 as eg
     torch.cuda.set_device(local)
     ekw = dict(capacity=args.capacity, chunk=args.chunk, block_size=args.block_size, ctas_per_sm=args.ctas_per_sm,
-               use_graph=args.graph)
+               use_graph=args.graph, inter_batch=args.inter_batch)
     eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], precision=args.precision, **ekw)
     eng.set_phantoms(ps)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
@@ -600,7 +602,7 @@ def main():
     H = int(args.histories)
     K, Wm = args.steps, args.warmup
     ekw = dict(capacity=args.capacity, chunk=args.chunk, howfarless=int(args.howfarless), block_size=args.block_size,
-               ctas_per_sm=args.ctas_per_sm, use_graph=args.graph)
+               ctas_per_sm=args.ctas_per_sm, use_graph=args.graph, inter_batch=args.inter_batch)
     eng = eg.DoseEngine(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], precision=args.precision, **ekw)
     eng.set_geometry(wl["geometry"])
     eng.set_source(wl["source"])

@@ -3565,6 +3565,17 @@ int egsgpu_run_noalloc(egsgpu_handle *h, long long first, long long n, uint32_t 
     if (h->cfg.bca_algorithm != 0) { h->err = "egsgpu_run_noalloc uses EXACT boundary crossing only"; return EGSGPU_ERR_ARG; }
     if (h->cfg.howfarless > 0) { h->err = "egsgpu_run_noalloc transports voxel by voxel only (no HOWFARLESS)"; return EGSGPU_ERR_ARG; }
     if (h->cfg.fp64_near_faces > 0) { h->err = "egsgpu_run_noalloc runs the default FP32 step (no fp64_near_faces)"; return EGSGPU_ERR_ARG; }
+    // The call synchronises its stream every round and runs as many rounds as
+    // the histories need, so it cannot be recorded into a graph: refuse a
+    // capturing stream before any other CUDA call, leaving the capture valid.
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    const cudaError_t ce = cudaStreamIsCapturing((cudaStream_t)stream, &cs);
+    if (ce != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+        if (ce != cudaSuccess) cudaGetLastError();
+        h->err = "egsgpu_run_noalloc cannot run on a capturing stream (it synchronises the stream every "
+                 "wavefront round)";
+        return EGSGPU_ERR_STATE;
+    }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) { h->err = "no current CUDA device"; return EGSGPU_ERR_CUDA; }
     unsigned char *scratch = nullptr;

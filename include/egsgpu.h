@@ -317,9 +317,11 @@ int egsgpu_combine_checkpoints(const void *a, size_t na, const void *b, size_t n
  * learn whether the queues have drained, and returns after the work
  * completes.  Block size, CTAs per SM and interaction batching are taken
  * from the handle's configuration as egsgpu_run takes them; the HOWFARLESS
- * and PRESTA-I options are refused (EGSGPU_ERR_ARG).  The first call on each
- * device looks up the array's device address with cudaGetSymbolAddress;
- * make that first call before any stream capture.  Every call shares the
+ * and PRESTA-I options are refused (EGSGPU_ERR_ARG).  The call cannot be
+ * recorded into a CUDA graph: on a stream that is capturing it returns
+ * EGSGPU_ERR_STATE at once, before any other CUDA call, and the capture stays
+ * valid.  The first call on each device looks up the array's device address
+ * with cudaGetSymbolAddress.  Every call shares the
  * one array: calls that overlap on the GPU (from several threads, streams
  * or handles) race and must be serialised by the caller.  The handle's
  * media, geometry and source must have been set (those calls allocate). */

@@ -84,3 +84,30 @@ def test_noalloc_refuses_other_transport_modes(option):
         eng.run_noalloc(dose.data_ptr(), 10)
     assert ex.value.code == 1
     eng.close()
+
+
+def test_noalloc_refuses_a_capturing_stream():
+    # the call synchronises its stream every round, so it cannot be recorded
+    # into a graph: on a capturing stream it must refuse at once and leave the
+    # caller's capture valid
+    import torch
+    wl = W.water30(20)
+    eng = engine(wl, 32)
+    dose = torch.zeros(wl["geometry"].nvox, dtype=torch.float64, device="cuda")
+    eng.run_noalloc(dose.data_ptr(), 16, seed=3)
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    refused = None
+    with torch.cuda.graph(g, stream=side):
+        dose.mul_(2.0)   # the captured work: the graph must stay usable
+        try:
+            eng.run_noalloc(dose.data_ptr(), 16, seed=3, stream=side.cuda_stream)
+        except eg.EGSError as ex:
+            refused = ex
+    assert refused is not None and refused.code == 7 and "capturing" in str(refused)
+    before = dose.clone()
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(dose, 2.0 * before)
+    eng.close()

@@ -102,7 +102,8 @@ struct Params {
     unsigned *peak;                       // largest queue length seen (autotuner input)
     uint32_t seed;
     int requeue_lanes;                    // park survivors of warps this sparse (0 = never)
-    int inter_batch;                      // lanes due to interact before the warp samples them
+    int inter_batch;                      // electron lanes due to interact before the warp samples them
+    int inter_batch_p;                    // the same for photon lanes
 };
 
 // A warp whose queue is exhausted parks its particles in the next queue once
@@ -112,7 +113,7 @@ constexpr unsigned REQUEUE_MIN = 32768;
 constexpr int LSTACK = 6;   // per-thread LIFO depth for charged secondaries
 // A photon lane crosses up to this many voxels per iteration of the persistent
 // loop before the warp's bookkeeping (refill, interaction batching) runs again.
-constexpr int PHOTON_HOPS = 8;
+constexpr int PHOTON_HOPS = 16;
 constexpr int INTER_MAXWAIT = 24;   // longest wait of a lane due to interact
 // Random numbers made present ahead of an electron step or an interaction
 // batch: a PRESTA-II step with the q-surface sampler takes 11 (two
@@ -756,7 +757,7 @@ __global__ void __launch_bounds__(MAX_BLOCK, sizeof(Real) == 4 ? 8 : 1) k_photon
             bool batch = false;
             if (pend) {
                 ++inter_wait;
-                batch = __popc(pend) >= min(P.inter_batch, __popc(live)) || inter_wait > INTER_MAXWAIT;
+                batch = __popc(pend) >= min(P.inter_batch_p, __popc(live)) || inter_wait > INTER_MAXWAIT;
             }
             if (batch) {
                 inter_wait = 0;
@@ -2533,6 +2534,7 @@ struct Engine : EngineBase {
         P.seed = seed;
         P.requeue_lanes = cfg.requeue_lanes > 0 ? cfg.requeue_lanes : 0;
         P.inter_batch = cfg.inter_batch > 0 ? std::min(cfg.inter_batch, 32) : (cfg.inter_batch < 0 ? 1 : 8);
+        P.inter_batch_p = cfg.inter_batch > 0 ? std::min(cfg.inter_batch, 32) : (cfg.inter_batch < 0 ? 1 : 12);
         if (Multi) {
             P.probs = (const Geom<Real> *)d_probs.p; P.pseeds = (const uint32_t *)d_pseeds.p;
             P.psrc = (const Source *)d_psrc.p; P.pvoff = (const int *)d_pvoff.p;
@@ -2878,6 +2880,7 @@ struct Engine : EngineBase {
         P.seed = seed;
         P.requeue_lanes = 0;
         P.inter_batch = cfg.inter_batch > 0 ? std::min(cfg.inter_batch, 32) : (cfg.inter_batch < 0 ? 1 : 8);
+        P.inter_batch_p = cfg.inter_batch > 0 ? std::min(cfg.inter_batch, 32) : (cfg.inter_batch < 0 ? 1 : 12);
         // the array keeps the previous call's contents: clear the counters
         CK(cudaMemsetAsync(scratch, 0, 1024, st));
         CK(set_caps(st));

@@ -58,8 +58,8 @@ typedef struct {
                              with CUDA events around every kernel.  Graphs give
                              no per-kernel timing; results are identical */
     int inter_batch;      /* lanes of a warp due to interact before their interactions
-                             are sampled together; 0 = default (8), -1 = immediately
-                             (results are identical either way) */
+                             are sampled together; 0 = default (8 electron, 12 photon
+                             lanes), -1 = immediately (results are identical either way) */
     int howfarless;       /* 1: DOSXYZnrc HOWFARLESS transport (ihowfarless,
                              user_codes/dosxyznrc/dosxyznrc.mortran:425-455) for a
                              homogeneous phantom: particles see only its outer

@@ -736,31 +736,45 @@ def main():
     if rank == 0 and not args.no_fp64 and args.precision == 32:
         # the plain FP64 GPU form on the same problem, timed the same way
         # (CUDA events on the launching stream around 2 steps of H/10)
-        e64 = eg.DoseEngine(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], precision=64, **ekw)
-        e64.set_geometry(g)
-        e64.set_source(wl["source"])
         H64 = max(H // 10, 100000)
-        first = 0
-        e64.run(H64 // 4, nbatch=1, seed=seed0 + 2000, first=first)
-        first += H64 // 4
-        e64.reset()
-        torch.cuda.synchronize()
-        start.record()
-        for _ in range(2):
-            flush.zero_()
-            e64.run(H64, nbatch=1, seed=seed0 + 2000, first=first)
-            first += H64
-        stop.record()
-        torch.cuda.synchronize()
-        T64 = start.elapsed_time(stop) / 1e3
-        s64, s264, _ = e64.tallies()
-        sig64, _ = sigma_eff(s64, s264, 2)
-        eff64 = 1.0 / (sig64 * sig64 * T64) if sig64 else None
-        e64.close()
+
+        def side_leg(precision, seed, **extra):
+            e = eg.DoseEngine(wl["media"], ecut=wl["ecut"], pcut=wl["pcut"], precision=precision, **ekw, **extra)
+            e.set_geometry(g)
+            e.set_source(wl["source"])
+            first = 0
+            e.run(H64 // 4, nbatch=1, seed=seed, first=first)
+            first += H64 // 4
+            e.reset()
+            torch.cuda.synchronize()
+            start.record()
+            for _ in range(2):
+                flush.zero_()
+                e.run(H64, nbatch=1, seed=seed, first=first)
+                first += H64
+            stop.record()
+            torch.cuda.synchronize()
+            t = start.elapsed_time(stop) / 1e3
+            s_, s2_, _ = e.tallies()
+            sig_, _ = sigma_eff(s_, s2_, 2)
+            pr = e.profile()
+            e.close()
+            return t, (1.0 / (sig_ * sig_ * t) if sig_ else None), pr
+
+        T64, eff64, _ = side_leg(64, seed0 + 2000)
         line["fp64"] = {"value": 2 * H64 / T64, "unit": "histories/s", "dose_efficiency": eff64,
                         "histories_per_step": H64, "steps": 2, "timing": "CUDA events"}
         if eff and eff64:
             line["efficiency_ratio_fp32_over_fp64"] = eff / eff64
+        # the FP32 kernels with FP64 residual ranges and face distances near
+        # voxel faces (egsgpu_config.fp64_near_faces), timed the same way
+        Tnf, effnf, pnf = side_leg(32, seed0 + 2500, fp64_near_faces=1)
+        line["fp64_near_faces"] = {
+            "value": 2 * H64 / Tnf, "unit": "histories/s", "dose_efficiency": effnf, "histories_per_step": H64,
+            "steps": 2, "timing": "CUDA events",
+            "electron_steps_in_fp64": (pnf.get("electron_wide_steps", 0.0) / pnf["electron_steps"]
+                                       if pnf.get("electron_steps") else 0.0),
+            "efficiency_ratio_over_fp64": (effnf / eff64) if (effnf and eff64) else None}
         line["fp32_vs_fp64"] = fp32_vs_fp64(wl, eg, ekw, max(H // 100, 200000), seed0 + 3000)
     line["simt"] = simt_roofline(prof)
     line["clocks"] = clk.summary()

@@ -2233,8 +2233,9 @@ struct Engine : EngineBase {
     // device memory free when the handle first runs (2^27 on a GB300 with
     // nothing else resident: 37.6 GB in FP32).  Larger queues let the chunk
     // autotuner run more histories per wavefront, and each chunk ends in a few
-    // short, sparsely occupied rounds: slab64 runs 6% faster at 2^27 than at
-    // 2^25.  Results do not depend on the capacity.
+    // short, sparsely occupied rounds: a 64^3-voxel slab phantom under a
+    // 0.1-6 MeV photon field runs 6% faster at 2^27 than at 2^25.  Results do
+    // not depend on the capacity.
     unsigned default_capacity() {
         if (capacity > 0) return capacity;
         size_t fr = 0, tot = 0;

@@ -1,7 +1,8 @@
-// Device-side data layout, random numbers and interaction samplers of the
-// GB300 transport engine.  Templated on the transport precision Real
-// (float or double); tallies are always FP64 and the residual-range /
-// energy-loss arithmetic uses RT (FP64 in both precisions).
+// Device-side data layout and random numbers of the GB300 transport engine.
+// Templated on the transport precision Real (float or double); tallies are
+// always FP64.  The FP32 electron kernel can compute the residual range, the
+// energy loss and the face distances of steps near voxel faces in FP64
+// (egsgpu_config.fp64_near_faces; the `wide_*` routines of egs_transport.cu).
 // Paths in comments are relative to the EGSnrc HEN_HOUSE directory.
 #pragma once
 #include <cstdint>

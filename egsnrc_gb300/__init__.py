@@ -333,9 +333,15 @@ def checkpoint_arrays(blob):
 
 
 def default_config(**kw):
+    """egsgpu_default_config with the named fields of egsgpu_config replaced;
+    an unknown name raises TypeError (a ctypes structure would otherwise take
+    it as a plain attribute and the engine would never see it)."""
     cfg = Config()
     load_library().egsgpu_default_config(C.byref(cfg))
+    fields = {f[0] for f in Config._fields_}
     for k, v in kw.items():
+        if k not in fields:
+            raise TypeError("egsgpu_config has no field %r" % k)
         setattr(cfg, k, v)
     return cfg
 

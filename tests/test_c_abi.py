@@ -38,6 +38,14 @@ def test_default_config_is_the_reference_profile(L):
     assert (c.ecut, c.pcut, c.estepe, c.ximax, c.skindepth, c.precision) == (0.521, 0.010, 0.25, 0.5, 3.0, 32)
 
 
+def test_config_keywords_name_fields_of_the_c_struct(L):
+    c = eg.default_config(inter_batch=12, fp64_near_faces=1, capacity=1 << 20)
+    assert (c.inter_batch, c.fp64_near_faces, c.capacity) == (12, 1, 1 << 20)
+    # a misspelt name must not pass silently as a Python attribute
+    with pytest.raises(TypeError):
+        eg.default_config(inter_bach=12)
+
+
 def test_create_reports_missing_device_or_bad_args(L):
     h = C.c_void_p()
     c = eg.default_config()

@@ -1006,6 +1006,65 @@ inline double eloss_g(const EMedium &em, double step, double eke, double elke, i
 // ------------------------------------------------------------ PHOTON ----
 void push(Run &R, const Particle &c) { R.stack.push_back(c); R.T->pushes += 1; }
 
+// The energy samplers of the discrete electron and positron interactions,
+// shared by the transport below and by oracle_sample_interaction (which
+// checks them against their cross sections).
+// MOLLER (src/egsnrc.mortran:2599-2746): the fraction br of the kinetic
+// energy ekin of an electron of total energy peie given to the delta ray.
+double moller_br(Run &R, Particle &p, const Medium &m, double ekin, double peie) {
+    double t0 = ekin / RM, e0 = t0 + 1, extrae = peie - m.thmoll, e02 = e0 * e0;
+    double g2 = t0 * t0 / e02, g3 = (2 * t0 + 1) / e02, gmax = 1 + 1.25 * g2, br, rejf4, r28;
+    do {
+        double r27 = rnd(R, p);
+        br = m.te / (ekin - extrae * r27);
+        double rr = br / (1 - br);
+        r28 = rnd(R, p);
+        rejf4 = 1 + g2 * br * br + rr * (rr - g3);
+        r28 = gmax * r28;
+    } while (!(r28 <= rejf4));
+    return br;
+}
+// BHABHA (:229-307): the fraction br of the positron's kinetic energy ekin
+// given to the electron, before PEGS's swap of the two (br >= 1/2).
+double bhabha_br(Run &R, Particle &p, const Medium &m, double ekin) {
+    double t0 = ekin / RM, e0 = t0 + 1.;
+    double yy = 1. / (t0 + 2.), e02 = e0 * e0, beta2 = (e02 - 1.) / e02;
+    double ep0 = m.te / ekin, ep0c = 1. - ep0, y2 = yy * yy, yp = 1. - 2. * yy, yp2 = yp * yp;
+    double b4 = yp2 * yp, b3 = b4 + yp2, b2 = yp * (3. + y2), b1 = 2. - y2, br, rejf2, r04;
+    do {
+        double r03 = rnd(R, p);
+        br = ep0 / (1. - ep0c * r03);
+        r04 = rnd(R, p);
+        rejf2 = (1.0 - beta2 * br * (b1 - br * (b2 - br * (b3 - br * b4))));
+    } while (!(r04 <= rejf2));
+    return br;
+}
+// BREMS (:312-524), Bethe-Heitler with the PEGS4 screening fits: the photon
+// energy esg from an electron of total energy eie2 (kinetic ekin, elke =
+// log ekin) with screening-fit columns l, l1.
+double brems_k(Run &R, Particle &p, const Medium &m, double eie2, double ekin, double elke, int l, int l1) {
+    double peie2 = eie2, brmin = m.ap / ekin, waux = elke - m.log_ap;
+    double esg, pese, ese, r07, rejf;
+    do {
+        double r06 = rnd(R, p);
+        r07 = rnd(R, p);
+        double br = brmin * std::exp(r06 * waux);
+        esg = ekin * br;
+        pese = peie2 - esg;
+        ese = pese;
+        double delta = esg / eie2 / ese * m.delcm, aux = ese / eie2, phi1, phi2;
+        if (delta < 1) {
+            phi1 = m.dl[0][l] + delta * (m.dl[1][l] + delta * m.dl[2][l]);
+            phi2 = m.dl[0][l1] + delta * (m.dl[1][l1] + delta * m.dl[2][l1]);
+        } else {
+            phi1 = m.dl[3][l] + m.dl[4][l] * std::log(delta + m.dl[5][l]);
+            phi2 = phi1;
+        }
+        rejf = (1 + aux * aux) * phi1 - 2 * aux * phi2 / 3;
+    } while (!(r07 < rejf));
+    return esg;
+}
+
 void photon(Run &R) {
     Oracle &O = *R.O;
     const Geometry &G = O.G;
@@ -1354,16 +1413,7 @@ newelectron:
                 // MOLLER (:2599-2746)
                 double peie2 = p.E, pekin = peie2 - RM, ekin = pekin;
                 if (ekin <= 2 * m.te) goto newelectron;
-                double t0 = ekin / RM, e0 = t0 + 1, extrae = peie2 - m.thmoll, e02 = e0 * e0;
-                double g2 = t0 * t0 / e02, g3 = (2 * t0 + 1) / e02, gmax = 1 + 1.25 * g2, br, rejf4, r28;
-                do {
-                    double r27 = rnd(R, p);
-                    br = m.te / (ekin - extrae * r27);
-                    double rr = br / (1 - br);
-                    r28 = rnd(R, p);
-                    rejf4 = 1 + g2 * br * br + rr * (rr - g3);
-                    r28 = gmax * r28;
-                } while (!(r28 <= rejf4));
+                double br = moller_br(R, p, m, ekin, peie2);
                 double pekse2 = br * ekin, pese1 = peie2 - pekse2, pese2 = pekse2 + RM;
                 double h1 = (peie2 + RM) / pekin;
                 double dcosth = h1 * (pese1 - RM) / (pese1 + RM);
@@ -1389,16 +1439,8 @@ newelectron:
                 double pbr2 = m.pbr21[lelke - 1] * elke + m.pbr20[lelke - 1];
                 if (r25 < pbr2) {
                     // BHABHA (:229-307)
-                    double peip = p.E, pekin = peip - RM, ekin = pekin, t0 = ekin / RM, e0 = t0 + 1.;
-                    double yy = 1. / (t0 + 2.), e02 = e0 * e0, beta2 = (e02 - 1.) / e02;
-                    double ep0 = m.te / ekin, ep0c = 1. - ep0, y2 = yy * yy, yp = 1. - 2. * yy, yp2 = yp * yp;
-                    double b4 = yp2 * yp, b3 = b4 + yp2, b2 = yp * (3. + y2), b1 = 2. - y2, br, rejf2, r04;
-                    do {
-                        double r03 = rnd(R, p);
-                        br = ep0 / (1. - ep0c * r03);
-                        r04 = rnd(R, p);
-                        rejf2 = (1.0 - beta2 * br * (b1 - br * (b2 - br * (b3 - br * b4))));
-                    } while (!(r04 <= rejf2));
+                    double peip = p.E, pekin = peip - RM, ekin = pekin;
+                    double br = bhabha_br(R, p, m, ekin);
                     int iq_np = 1, iq_new = -1;
                     if (!(br < 0.5)) { iq_np = -1; iq_new = 1; br = 1. - br; }
                     br = std::max(br, 0.0);
@@ -1453,7 +1495,7 @@ newelectron:
         }
         // BREMS (:312-524), BH cross section, KM angle
         {
-            double peie2 = p.E, eie2 = peie2, ekin = peie2 - RM, brmin = m.ap / ekin, waux = elke - m.log_ap;
+            double peie2 = p.E, eie2 = peie2, ekin = peie2 - RM;
             int l = (eie2 < 50.0) ? 0 : 2, l1 = l + 1;
             double a = p.u, b = p.v, c = p.w, sinpsi = a * a + b * b, sindel = 0, cosdel = 0;
             if (sinpsi > 1e-20) { sinpsi = std::sqrt(sinpsi); sindel = b / sinpsi; cosdel = a / sinpsi; }
@@ -1461,24 +1503,8 @@ newelectron:
             double beta = std::sqrt((tteie - 1) * (tteie + 1)) / tteie;
             double y2max = 2 * beta * (1 + beta) * tteie * tteie, y2maxi = 1 / y2max;
             double z2max = y2max + 1, z2maxi = std::sqrt(z2max);
-            double esg, pese, ese, r07, rejf;
-            do {
-                double r06 = rnd(R, p);
-                r07 = rnd(R, p);
-                double br = brmin * std::exp(r06 * waux);
-                esg = ekin * br;
-                pese = peie2 - esg;
-                ese = pese;
-                double delta = esg / eie2 / ese * m.delcm, aux = ese / eie2, phi1, phi2;
-                if (delta < 1) {
-                    phi1 = m.dl[0][l] + delta * (m.dl[1][l] + delta * m.dl[2][l]);
-                    phi2 = m.dl[0][l1] + delta * (m.dl[1][l1] + delta * m.dl[2][l1]);
-                } else {
-                    phi1 = m.dl[3][l] + m.dl[4][l] * std::log(delta + m.dl[5][l]);
-                    phi2 = phi1;
-                }
-                rejf = (1 + aux * aux) * phi1 - 2 * aux * phi2 / 3;
-            } while (!(r07 < rejf));
+            const double esg = brems_k(R, p, m, eie2, ekin, elke, l, l1);
+            const double pese = peie2 - esg, ese = pese;
             double ttese = ese / RM, esedei = ttese / tteie, rjarg1 = 1 + esedei * esedei, rjarg2 = rjarg1 + 2 * esedei;
             double aux = 2 * ese * tteie / esg;
             aux = aux * aux;
@@ -1736,6 +1762,10 @@ int oracle_geometry_query(oracle_handle *h, int op, long long n, const int32_t *
 //   kind 2  photo-electron direction ($SELECT-PHOTOELECTRON-DIRECTION) of a
 //           photo-electron of total energy E: out = {cos theta}
 //   kind 3  pair production:                  out = {electron total energy, positron total energy}
+//   kind 4  Moller, electron of total energy E: out = {fraction of the kinetic energy to the delta ray}
+//   kind 5  Bhabha, positron of total energy E: out = {fraction of the kinetic energy to the electron,
+//           before the swap that keeps the larger share on the positron}
+//   kind 6  bremsstrahlung, electron of total energy E: out = {photon energy}
 // out has 3 values per interaction (unused ones 0).
 int oracle_sample_interaction(oracle_handle *h, int kind, int med, double E, long long n, uint32_t seed,
                               double *out) {
@@ -1783,11 +1813,32 @@ int oracle_sample_interaction(oracle_handle *h, int kind, int med, double E, lon
             pair(R, p, m, second);
             o[0] = p.iq < 0 ? p.E : second.E;
             o[1] = p.iq < 0 ? second.E : p.E;
+        } else if (kind == 4) {   // Moller, electron of total energy E (E > thmoll)
+            if (!(E > m.thmoll)) return 1;
+            o[0] = moller_br(R, p, m, E - RM, E);
+        } else if (kind == 5) {   // Bhabha, positron of total energy E (kinetic > te)
+            if (!(E - RM > m.te)) return 1;
+            o[0] = bhabha_br(R, p, m, E - RM);
+        } else if (kind == 6) {   // bremsstrahlung photon energy, electron of total energy E (kinetic > ap)
+            const double ekin = E - RM;
+            if (!(ekin > m.ap)) return 1;
+            const int l = (E < 50.0) ? 0 : 2;
+            o[0] = brems_k(R, p, m, E, ekin, std::log(ekin), l, l + 1);
         } else {
             return 1;
         }
     }
     return R.errors ? 2 : 0;
+}
+
+// Thresholds of medium `med` (HATCH, from PEGS4): out[3] = {te (the Moller
+// and Bhabha delta-ray threshold, kinetic), thmoll (the Moller threshold,
+// total energy), ap (the bremsstrahlung photon threshold)}, MeV.
+int oracle_medium_thresholds(oracle_handle *h, int med, double *out) {
+    if (med < 0 || med >= (int)h->O.H.media.size()) return 1;
+    const Medium &m = h->O.H.media[med];
+    out[0] = m.te; out[1] = m.thmoll; out[2] = m.ap;
+    return 0;
 }
 
 // Pair-production constants of medium `med` (HATCH, from PEGS4): out[51] =

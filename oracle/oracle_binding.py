@@ -75,6 +75,7 @@ def _declare(L):
         L.oracle_sample_source.argtypes = [vp, i64, i64, C.c_uint32, dp]
         L.oracle_sample_interaction.argtypes = [vp, C.c_int, C.c_int, C.c_double, i64, C.c_uint32, dp]
         L.oracle_medium_pair.argtypes = [vp, C.c_int, dp]
+        L.oracle_medium_thresholds.argtypes = [vp, C.c_int, dp]
     return L
 
 
@@ -187,13 +188,21 @@ class Oracle:
 
     def sample_interaction(self, kind, med, energy, n, seed=1):
         """n samples of one interaction sampler alone (kind 0 Klein-Nishina on
-        free electrons, 1 bound Compton, 2 photo-electron direction, 3 pair);
-        rows of 3 values as oracle_sample_interaction describes."""
+        free electrons, 1 bound Compton, 2 photo-electron direction, 3 pair,
+        4 Moller, 5 Bhabha, 6 bremsstrahlung); rows of 3 values as
+        oracle_sample_interaction describes."""
         out = np.zeros((n, 3))
         rc = self.L.oracle_sample_interaction(self.h, int(kind), int(med), float(energy), int(n), int(seed), _dp(out))
         if rc:
             raise RuntimeError("oracle sampler error %d" % rc)
         return out
+
+    def thresholds(self, med):
+        """te (kinetic delta-ray threshold), thmoll (Moller threshold, total
+        energy) and ap (bremsstrahlung photon threshold) of medium med, MeV."""
+        out = np.zeros(3)
+        assert self.L.oracle_medium_thresholds(self.h, int(med), _dp(out)) == 0
+        return float(out[0]), float(out[1]), float(out[2])
 
     def pair_constants(self, med):
         """dl[6][8], delcm and bpar[2] of medium med."""

@@ -18,6 +18,21 @@ pin the GPU samplers too.
   PAIR forms it, dsigma/db ~ (1 - 2m/E)^2 (1 - 2b)^2 A(delta) + B(delta), A and B the
   PEGS4 screening fits dl1..dl6 (l = 4, 5) of the medium, each taken as 0 where
   its fit is negative (large delta near threshold).
+* Moller (MOLLER, src/egsnrc.mortran:2599-2746), the energy fraction eps of
+  the delta ray, eps in [te/T, 1/2], t = T/m:
+  dsigma/deps ~ 1/eps^2 + 1/(1 - eps)^2 + (t/(t+1))^2 - (2t+1)/(t+1)^2 / (eps (1 - eps)).
+* Bhabha (BHABHA, :229-307), the energy fraction eps of the electron before
+  the swap, eps in [te/T, 1], y = 1/(gamma + 1):
+  dsigma/deps ~ (1/eps^2) [1/beta^2 - B1 eps + B2 eps^2 - B3 eps^3 + B4 eps^4],
+  B1 = 2 - y^2, B2 = (1 - 2y)(3 + y^2), B3 = (1 - 2y)^2 (2 - 2y), B4 = (1 - 2y)^3.
+* Bethe-Heitler bremsstrahlung (BREMS, :312-524), photon energy k in [AP, T]:
+  dsigma/dk ~ (1/k) [(1 + (E'/E)^2) phi1(delta) - (2/3)(E'/E) phi2(delta)],
+  E' = E - k, delta = k delcm / (E E'), phi1, phi2 the PEGS4 screening fits
+  of the medium (columns 0, 1 below 50 MeV, 2, 3 above); the bracket is
+  taken as 0 where the fits make it negative (a rejection sampler cannot
+  produce negative density).
+Each is histogrammed in the variable in which its sampler's proposal is
+uniform (1/eps or log k), so that the bins are populated evenly.
 """
 import numpy as np
 import pytest
@@ -132,3 +147,66 @@ def test_bound_compton_limits(ora):
     bd = ora.sample_interaction(1, 0, 5.0, N, seed=6)
     assert abs(bd[:, 0].mean() / kn[:, 0].mean() - 1) < 2e-3
     assert np.all(bd[:, 2] >= 0) and bd[:, 2].max() < 1e-3   # water: O K shell 0.54 keV
+
+
+@pytest.mark.parametrize("kinetic", [0.1, 1.0, 10.0])
+def test_moller_delta_ray_energy(ora, kinetic):
+    te, thmoll, _ = ora.thresholds(0)
+    t = kinetic / RM
+    e_min = te / kinetic
+    eps = ora.sample_interaction(4, 0, kinetic + RM, N, seed=7)[:, 0]
+    assert eps.min() >= e_min * (1 - 1e-12) and eps.max() <= 0.5 + 1e-12
+    a = 1 / e_min - 2   # y = (1/e_min - 1/eps) / a is uniform under the 1/eps^2 proposal
+
+    def pdf(y):
+        e = 1 / (1 / e_min - a * y)
+        f = 1 / e ** 2 + 1 / (1 - e) ** 2 + (t / (t + 1)) ** 2 - (2 * t + 1) / (t + 1) ** 2 / (e * (1 - e))
+        return f * e * e
+    stat, dof, p = gof((1 / e_min - 1 / eps) / a, pdf, 0.0, 1.0)
+    assert p > 1e-3, (kinetic, stat, dof, p)
+
+
+@pytest.mark.parametrize("kinetic", [0.1, 1.0, 10.0])
+def test_bhabha_electron_energy(ora, kinetic):
+    te, _, _ = ora.thresholds(0)
+    gamma = kinetic / RM + 1
+    beta2 = 1 - 1 / gamma ** 2
+    y = 1 / (gamma + 1)
+    b1, b2 = 2 - y * y, (1 - 2 * y) * (3 + y * y)
+    b3, b4 = (1 - 2 * y) ** 2 * (2 - 2 * y), (1 - 2 * y) ** 3
+    e_min = te / kinetic
+    eps = ora.sample_interaction(5, 0, kinetic + RM, N, seed=8)[:, 0]
+    assert eps.min() >= e_min * (1 - 1e-12) and eps.max() <= 1 + 1e-12
+    a = 1 / e_min - 1
+
+    def pdf(u):
+        e = 1 / (1 / e_min - a * u)
+        f = (1 / beta2 - b1 * e + b2 * e ** 2 - b3 * e ** 3 + b4 * e ** 4) / e ** 2
+        return f * e * e
+    stat, dof, p = gof((1 / e_min - 1 / eps) / a, pdf, 0.0, 1.0)
+    assert p > 1e-3, (kinetic, stat, dof, p)
+
+
+@pytest.mark.parametrize("med,kinetic", [(0, 1.0), (0, 5.0), (1, 20.0), (0, 60.0)])
+def test_bremsstrahlung_photon_energy(ora, med, kinetic):
+    dl, delcm, _ = ora.pair_constants(med)
+    _, _, ap = ora.thresholds(med)
+    E = kinetic + RM
+    l, l1 = (0, 1) if E < 50 else (2, 3)
+    k = ora.sample_interaction(6, med, E, N, seed=9)[:, 0]
+    assert k.min() >= ap * (1 - 1e-12) and k.max() <= kinetic * (1 + 1e-12)
+    span = np.log(kinetic / ap)   # y = log(k/ap)/span is uniform under the 1/k proposal
+
+    def phi(col, delta):
+        if delta < 1:
+            return dl[0][col] + delta * (dl[1][col] + delta * dl[2][col])
+        return dl[3][l] + dl[4][l] * np.log(delta + dl[5][l])
+
+    def pdf(y):
+        kk = ap * np.exp(y * span)
+        ep = E - kk
+        delta = kk * delcm / (E * ep)
+        aux = ep / E
+        return max((1 + aux * aux) * phi(l, delta) - 2 * aux * phi(l1, delta) / 3, 0.0)
+    stat, dof, p = gof(np.log(k / ap) / span, pdf, 0.0, 1.0)
+    assert p > 1e-3, (med, kinetic, stat, dof, p)

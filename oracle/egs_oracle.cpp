@@ -1766,6 +1766,7 @@ int oracle_geometry_query(oracle_handle *h, int op, long long n, const int32_t *
 //   kind 5  Bhabha, positron of total energy E: out = {fraction of the kinetic energy to the electron,
 //           before the swap that keeps the larger share on the positron}
 //   kind 6  bremsstrahlung, electron of total energy E: out = {photon energy}
+//   kind 7  Rayleigh scattering, photon of energy E: out = {cos theta}
 // out has 3 values per interaction (unused ones 0).
 int oracle_sample_interaction(oracle_handle *h, int kind, int med, double E, long long n, uint32_t seed,
                               double *out) {
@@ -1819,6 +1820,15 @@ int oracle_sample_interaction(oracle_handle *h, int kind, int med, double E, lon
         } else if (kind == 5) {   // Bhabha, positron of total energy E (kinetic > te)
             if (!(E - RM > m.te)) return 1;
             o[0] = bhabha_br(R, p, m, E - RM);
+        } else if (kind == 7) {   // Rayleigh, photon of energy E: out = {cos theta}
+            PhotonCtx pc;
+            pc.gle = std::log(E);
+            pc.lgle = interval(pc.gle, m.ge1, m.ge0);
+            pc.cohfac = 1;
+            if (pc.lgle < 1 || pc.lgle > m.mge) return 1;
+            double costhe, sinthe;
+            rayleigh_sample(R, p, m, pc, costhe, sinthe);
+            o[0] = costhe;
         } else if (kind == 6) {   // bremsstrahlung photon energy, electron of total energy E (kinetic > ap)
             const double ekin = E - RM;
             if (!(ekin > m.ap)) return 1;
@@ -1838,6 +1848,17 @@ int oracle_medium_thresholds(oracle_handle *h, int med, double *out) {
     if (med < 0 || med >= (int)h->O.H.media.size()) return 1;
     const Medium &m = h->O.H.media[med];
     out[0] = m.te; out[1] = m.thmoll; out[2] = m.ap;
+    return 0;
+}
+
+// Composition of medium `med` (PEGS4): out[0] = number of elements n, then
+// Z_i (n values) and atoms per molecule p_i (n values); out holds 1 + 2 nmax.
+int oracle_medium_elements(oracle_handle *h, int med, int nmax, double *out) {
+    if (med < 0 || med >= (int)h->O.H.media.size()) return 1;
+    const Medium &m = h->O.H.media[med];
+    if (m.nne > nmax) return 1;
+    out[0] = m.nne;
+    for (int i = 0; i < m.nne; ++i) { out[1 + i] = m.zelem[i]; out[1 + m.nne + i] = m.pz[i]; }
     return 0;
 }
 

@@ -76,6 +76,7 @@ def _declare(L):
         L.oracle_sample_interaction.argtypes = [vp, C.c_int, C.c_int, C.c_double, i64, C.c_uint32, dp]
         L.oracle_medium_pair.argtypes = [vp, C.c_int, dp]
         L.oracle_medium_thresholds.argtypes = [vp, C.c_int, dp]
+        L.oracle_medium_elements.argtypes = [vp, C.c_int, C.c_int, dp]
     return L
 
 
@@ -189,7 +190,7 @@ class Oracle:
     def sample_interaction(self, kind, med, energy, n, seed=1):
         """n samples of one interaction sampler alone (kind 0 Klein-Nishina on
         free electrons, 1 bound Compton, 2 photo-electron direction, 3 pair,
-        4 Moller, 5 Bhabha, 6 bremsstrahlung); rows of 3 values as
+        4 Moller, 5 Bhabha, 6 bremsstrahlung, 7 Rayleigh); rows of 3 values as
         oracle_sample_interaction describes."""
         out = np.zeros((n, 3))
         rc = self.L.oracle_sample_interaction(self.h, int(kind), int(med), float(energy), int(n), int(seed), _dp(out))
@@ -203,6 +204,14 @@ class Oracle:
         out = np.zeros(3)
         assert self.L.oracle_medium_thresholds(self.h, int(med), _dp(out)) == 0
         return float(out[0]), float(out[1]), float(out[2])
+
+    def elements(self, med):
+        """Atomic numbers and atoms per molecule of medium med (PEGS4)."""
+        nmax = 32
+        out = np.zeros(1 + 2 * nmax)
+        assert self.L.oracle_medium_elements(self.h, int(med), nmax, _dp(out)) == 0
+        n = int(out[0])
+        return out[1:1 + n].astype(int), out[1 + n:1 + 2 * n].copy()
 
     def pair_constants(self, med):
         """dl[6][8], delcm and bpar[2] of medium med."""

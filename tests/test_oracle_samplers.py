@@ -31,15 +31,26 @@ pin the GPU samplers too.
   of the medium (columns 0, 1 below 50 MeV, 2, 3 above); the bracket is
   taken as 0 where the fits make it negative (a rejection sampler cannot
   produce negative density).
+* Rayleigh scattering (egs_rayleigh_sampling, src/egsnrc.mortran:8559-8590,
+  prepare_rayleigh_data :8593-8726), photon of energy E:
+  dsigma/dcos ~ (1 + cos^2) F^2(x), x = E sin(theta/2)/hc, with F^2 the
+  independent-atom molecular form factor sum p_i F_i^2 of the medium's
+  elements from pgs4form.dat, interpolated as a power law in x between the
+  tabulated points as PEGS does.
 Each is histogrammed in the variable in which its sampler's proposal is
-uniform (1/eps or log k), so that the bins are populated evenly.
+uniform (1/eps, log k, or the cumulative of F^2 in x^2), so that the bins are
+populated evenly.
 """
+import os
+
 import numpy as np
 import pytest
 from scipy import integrate
 from scipy.stats import chi2 as chi2_dist
 
 from oracle.oracle_binding import Oracle
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 RM = 0.5109989461
 N = 200000
@@ -210,3 +221,51 @@ def test_bremsstrahlung_photon_energy(ora, med, kinetic):
         return max((1 + aux * aux) * phi(l, delta) - 2 * aux * phi(l1, delta) / 3, 0.0)
     stat, dof, p = gof(np.log(k / ap) / span, pdf, 0.0, 1.0)
     assert p > 1e-3, (med, kinetic, stat, dof, p)
+
+
+HC_INV = 80.65506856998   # 1/(hc) in 1/(MeV Angstrom), as egs_rayleigh_sampling has it
+TWICE_HC2 = 0.000307444456
+
+
+def molecular_form_factor(z, pz):
+    """Grid x (1/Angstrom) and F(x) = sqrt(sum_i p_i F_i(x)^2) from the raw
+    pgs4form.dat (100 x values, then 100 values per element Z = 1..100)."""
+    vals = np.array(open(os.path.join(ROOT, "egsnrc_gb300", "data", "pgs4form.dat")).read().split(), dtype=float)
+    x = vals[:100].copy()
+    aff = vals[100:100 + 100 * 100].reshape(100, 100)
+    f = np.sqrt(sum(p * aff[int(zz) - 1] ** 2 for zz, p in zip(z, pz)))
+    if x[0] < 1e-6:
+        x[0] = 1e-4
+    f[f == 0] = 1e-30
+    return x, f
+
+
+@pytest.mark.parametrize("med,energy", [(0, 0.02), (0, 0.05), (0, 0.1), (0, 0.5), (1, 0.03), (1, 0.1)])
+def test_rayleigh_angle(ora, med, energy):
+    z, pz = ora.elements(med)
+    x, f = molecular_form_factor(z, pz)
+    b = np.log(f[1:] / f[:-1]) / np.log(x[1:] / x[:-1])   # F = f_i (x/x_i)^b_i on [x_i, x_i+1)
+    coef = f[:-1] ** 2 * x[:-1] ** (-2 * b) / (b + 1)
+    cum = np.concatenate([[0.0], np.cumsum(coef * (x[1:] ** (2 * b + 2) - x[:-1] ** (2 * b + 2)))])
+
+    def cdf(xx):   # integral of F^2 d(x^2) from x_0 to xx
+        i = np.clip(np.searchsorted(x, xx, side="right") - 1, 0, len(b) - 1)
+        return cum[i] + coef[i] * (xx ** (2 * b[i] + 2) - x[i] ** (2 * b[i] + 2))
+
+    def inverse(pp):
+        i = np.clip(np.searchsorted(cum, pp, side="right") - 1, 0, len(b) - 1)
+        return (x[i] ** (2 * b[i] + 2) + (pp - cum[i]) / coef[i]) ** (1 / (2 * b[i] + 2))
+
+    xmax = HC_INV * energy
+    ptot = cdf(xmax)
+    c = ora.sample_interaction(7, med, energy, N, seed=10)[:, 0]
+    assert c.min() >= -1 - 1e-12 and c.max() <= 1 + 1e-12
+    xs = energy * np.sqrt(np.maximum(1 - c, 0) / TWICE_HC2)
+    t = cdf(xs) / ptot   # uniform under the F^2 proposal
+
+    def pdf(u):
+        xx = inverse(u * ptot)
+        cc = 1 - TWICE_HC2 * (xx / energy) ** 2
+        return 1 + cc * cc
+    stat, dof, p = gof(t, pdf, 0.0, 1.0)
+    assert p > 1e-3, (med, energy, stat, dof, p)

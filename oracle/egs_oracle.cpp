@@ -1039,6 +1039,19 @@ double bhabha_br(Run &R, Particle &p, const Medium &m, double ekin) {
     } while (!(r04 <= rejf2));
     return br;
 }
+// ANNIH in flight (:70-182): the energy fraction ep of the first photon, for
+// a = (positron total energy + m)/m, ep0 = 1/(a + sqrt(a (a - 2))) and
+// wsamp = log((1 - ep0)/ep0).
+double annih_ep(Run &R, Particle &p, double a, double ep0, double wsamp) {
+    double ep, r02, rejf;
+    do {
+        double r01 = rnd(R, p);
+        ep = ep0 * std::exp(r01 * wsamp);
+        r02 = rnd(R, p);
+        rejf = 1 - (ep * a - 1) * (ep * a - 1) / (ep * (a * a - 2));
+    } while (!(r02 <= rejf));
+    return ep;
+}
 // BREMS (:312-524), Bethe-Heitler with the PEGS4 screening fits: the photon
 // energy esg from an electron of total energy eie2 (kinetic ekin, elke =
 // log ekin) with screening-fit columns l, l1.
@@ -1466,13 +1479,8 @@ newelectron:
                 // ANNIH in flight (:70-182)
                 double pavip = p.E + RM, avip = pavip, a = avip / RM, g = a - 1.0, t = g - 1.0;
                 double pp = std::sqrt(a * t), pot = pp / t, ep0 = 1.0 / (a + pp), wsamp = std::log((1.0 - ep0) / ep0);
-                double aa = p.u, bb = p.v, cc = p.w, ep, r02, rejf;
-                do {
-                    double r01 = rnd(R, p);
-                    ep = ep0 * std::exp(r01 * wsamp);
-                    r02 = rnd(R, p);
-                    rejf = 1 - (ep * a - 1) * (ep * a - 1) / (ep * (a * a - 2));
-                } while (!(r02 <= rejf));
+                double aa = p.u, bb = p.v, cc = p.w;
+                const double ep = annih_ep(R, p, a, ep0, wsamp);
                 double esg1 = avip * ep;
                 Particle g1 = p;
                 g1.E = esg1; g1.iq = 0;
@@ -1767,6 +1775,8 @@ int oracle_geometry_query(oracle_handle *h, int op, long long n, const int32_t *
 //           before the swap that keeps the larger share on the positron}
 //   kind 6  bremsstrahlung, electron of total energy E: out = {photon energy}
 //   kind 7  Rayleigh scattering, photon of energy E: out = {cos theta}
+//   kind 8  two-photon annihilation in flight, positron of total energy E:
+//           out = {energy fraction of the first photon}
 // out has 3 values per interaction (unused ones 0).
 int oracle_sample_interaction(oracle_handle *h, int kind, int med, double E, long long n, uint32_t seed,
                               double *out) {
@@ -1820,6 +1830,11 @@ int oracle_sample_interaction(oracle_handle *h, int kind, int med, double E, lon
         } else if (kind == 5) {   // Bhabha, positron of total energy E (kinetic > te)
             if (!(E - RM > m.te)) return 1;
             o[0] = bhabha_br(R, p, m, E - RM);
+        } else if (kind == 8) {   // annihilation in flight, positron of total energy E
+            const double a = (E + RM) / RM, g = a - 1.0, t = g - 1.0;
+            if (!(t > 0)) return 1;
+            const double pp = std::sqrt(a * t), ep0 = 1.0 / (a + pp), wsamp = std::log((1.0 - ep0) / ep0);
+            o[0] = annih_ep(R, p, a, ep0, wsamp);
         } else if (kind == 7) {   // Rayleigh, photon of energy E: out = {cos theta}
             PhotonCtx pc;
             pc.gle = std::log(E);

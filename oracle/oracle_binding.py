@@ -190,7 +190,8 @@ class Oracle:
     def sample_interaction(self, kind, med, energy, n, seed=1):
         """n samples of one interaction sampler alone (kind 0 Klein-Nishina on
         free electrons, 1 bound Compton, 2 photo-electron direction, 3 pair,
-        4 Moller, 5 Bhabha, 6 bremsstrahlung, 7 Rayleigh); rows of 3 values as
+        4 Moller, 5 Bhabha, 6 bremsstrahlung, 7 Rayleigh, 8 annihilation in
+        flight); rows of 3 values as
         oracle_sample_interaction describes."""
         out = np.zeros((n, 3))
         rc = self.L.oracle_sample_interaction(self.h, int(kind), int(med), float(energy), int(n), int(seed), _dp(out))

@@ -31,6 +31,11 @@ pin the GPU samplers too.
   of the medium (columns 0, 1 below 50 MeV, 2, 3 above); the bracket is
   taken as 0 where the fits make it negative (a rejection sampler cannot
   produce negative density).
+* Two-photon annihilation in flight (ANNIH, :70-182; Heitler), positron of
+  total energy gamma m on an electron at rest, photon energy fractions eps
+  and 1 - eps of (gamma + 1) m, the smaller one folded to [eps0, 1/2]:
+  dsigma/deps ~ S(eps) + S(1 - eps), S(e) = -(gamma+1)^2 + (gamma^2 + 4 gamma + 1)/e - 1/e^2,
+  eps0 = (1 - sqrt((gamma - 1)/(gamma + 1)))/2.
 * Rayleigh scattering (egs_rayleigh_sampling, src/egsnrc.mortran:8559-8590,
   prepare_rayleigh_data :8593-8726), photon of energy E:
   dsigma/dcos ~ (1 + cos^2) F^2(x), x = E sin(theta/2)/hc, with F^2 the
@@ -269,3 +274,22 @@ def test_rayleigh_angle(ora, med, energy):
         return 1 + cc * cc
     stat, dof, p = gof(t, pdf, 0.0, 1.0)
     assert p > 1e-3, (med, energy, stat, dof, p)
+
+
+@pytest.mark.parametrize("kinetic", [0.1, 1.0, 10.0])
+def test_annihilation_in_flight_photon_energy(ora, kinetic):
+    gamma = kinetic / RM + 1
+    eps0 = 0.5 * (1 - np.sqrt((gamma - 1) / (gamma + 1)))
+    eps = ora.sample_interaction(8, 0, kinetic + RM, N, seed=11)[:, 0]
+    assert eps.min() >= eps0 * (1 - 1e-9) and eps.max() <= (1 - eps0) * (1 + 1e-9)
+    e = np.minimum(eps, 1 - eps)
+    span = np.log(0.5 / eps0)   # y = log(e/eps0)/span: the 1/e proposal, folded
+
+    def s(v):
+        return -(gamma + 1) ** 2 + (gamma ** 2 + 4 * gamma + 1) / v - 1 / v ** 2
+
+    def pdf(y):
+        v = eps0 * np.exp(y * span)
+        return (s(v) + s(1 - v)) * v
+    stat, dof, p = gof(np.log(e / eps0) / span, pdf, 0.0, 1.0)
+    assert p > 1e-3, (kinetic, stat, dof, p)

@@ -185,7 +185,7 @@ struct Rng {
     __device__ inline void fill(uint32_t b) {
         reinterpret_cast<uint4 *>(c)[b & 3u] = philox_block(b, (uint32_t)sid, (uint32_t)(sid >> 32), seed, hist);
     }
-    // make the blocks holding the next k numbers (k <= 13) present.  The ten
+    // make the blocks holding the next k numbers (1 <= k <= 13) present.  The ten
     // rounds are inlined here (one copy per transport loop): a call to the
     // shared out-of-line block from this site measured 10-20% slower.
     __device__ inline void ahead(uint32_t k) {

@@ -4,6 +4,7 @@ codes (no exit, no fallback)."""
 import ctypes as C
 import os
 import re
+import subprocess
 
 import pytest
 
@@ -101,3 +102,38 @@ def test_combine_checkpoints_refuses_mismatches(L):
         eg.combine_checkpoints(a, a[:-8])
     n = C.c_size_t(0)
     assert L.egsgpu_combine_checkpoints(a, len(a), a, len(a), None, C.byref(n)) == 0 and n.value == len(a)
+
+
+C_CALLER = r"""
+#include <stdio.h>
+#include "egsgpu.h"
+int main(void) {
+    egsgpu_config c;
+    egsgpu_handle *h = 0;
+    int rc;
+    egsgpu_default_config(&c);
+    if (c.precision != 32) return 10;
+    c.precision = 16;
+    rc = egsgpu_create(&c, &h);
+    if (rc != EGSGPU_ERR_ARG || h) return 11;
+    if (!egsgpu_last_error(0)) return 12;
+    printf("%d\n", rc);
+    return 0;
+}
+"""
+
+
+def test_header_is_plain_c_and_links(L, tmp_path):
+    # the boundary is usable from C (the language of cgo, JNI and FFI
+    # bindings): the header compiles as strict C99 and a C program links
+    # against the library and calls it
+    src = tmp_path / "caller.c"
+    src.write_text(C_CALLER)
+    exe = tmp_path / "caller"
+    lib_dir = os.path.dirname(eg.library_path())
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I",
+                        os.path.join(ROOT, "include"), str(src), "-o", str(exe), "-L" + lib_dir, "-legsgpu",
+                        "-Wl,-rpath," + lib_dir], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.strip() == "1", (r.returncode, r.stdout, r.stderr)

@@ -155,8 +155,10 @@ __host__ __device__ inline uint64_t child_sid(uint64_t sid, uint32_t n, uint32_t
 // One Philox block, kept out of line: the generator is called from about a
 // hundred places in the transport kernels and inlining its ten rounds at each
 // would multiply the kernels' instruction footprint.
-// (internal linkage: each translation unit of the engine has its own copy)
-static __device__ __noinline__ uint4 philox_block(uint32_t b, uint32_t s0, uint32_t s1, uint32_t k0, uint32_t k1);
+// (internal linkage: each translation unit of the engine has its own copy;
+// host-callable so that the generator's window logic can be checked on a CPU)
+static __host__ __device__ __noinline__ uint4 philox_block(uint32_t b, uint32_t s0, uint32_t s1, uint32_t k0,
+                                                           uint32_t k1);
 
 // The generator keeps a window of the stream's next four Philox blocks
 // (block b in slot b & 3; `next` is one past the highest block held).  A
@@ -179,16 +181,16 @@ struct Rng {
         seed = o.seed; hist = o.hist; n = o.n; sid = o.sid; next = 0;
         return *this;
     }
-    __device__ void init(uint32_t s, uint32_t h, uint64_t id, uint32_t n0) {
+    __host__ __device__ void init(uint32_t s, uint32_t h, uint64_t id, uint32_t n0) {
         seed = s; hist = h; sid = id; n = n0; next = 0;
     }
-    __device__ inline void fill(uint32_t b) {
+    __host__ __device__ inline void fill(uint32_t b) {
         reinterpret_cast<uint4 *>(c)[b & 3u] = philox_block(b, (uint32_t)sid, (uint32_t)(sid >> 32), seed, hist);
     }
     // make the blocks holding the next k numbers (1 <= k <= 13) present.  The ten
     // rounds are inlined here (one copy per transport loop): a call to the
     // shared out-of-line block from this site measured 10-20% slower.
-    __device__ inline void ahead(uint32_t k) {
+    __host__ __device__ inline void ahead(uint32_t k) {
         const uint32_t b0 = n >> 2, b1 = (n + k - 1) >> 2;
         uint32_t b = next > b0 ? next : b0;
         for (; b <= b1; ++b) {
@@ -204,12 +206,12 @@ struct Rng {
     // generator state then lives in local memory around each call.  Sites that
     // take two numbers in a row call u2 (one call instead of two: +3% on
     // electron-dominated phantoms).
-    __device__ __noinline__ float u() { return draw(); }
-    __device__ __noinline__ float2 u2() {
+    __host__ __device__ __noinline__ float u() { return draw(); }
+    __host__ __device__ __noinline__ float2 u2() {
         float a = draw();
         return make_float2(a, draw());
     }
-    __device__ inline float draw() {
+    __host__ __device__ inline float draw() {
         const uint32_t b = n >> 2;
         // present: b < next, and b >= next - 4 since ahead() never runs more
         // than three blocks past the current one

@@ -51,7 +51,8 @@ namespace cg = cooperative_groups;
 
 namespace egsgpu {
 
-static __device__ __noinline__ uint4 philox_block(uint32_t b, uint32_t s0, uint32_t s1, uint32_t k0, uint32_t k1) {
+static __host__ __device__ __noinline__ uint4 philox_block(uint32_t b, uint32_t s0, uint32_t s1, uint32_t k0,
+                                                           uint32_t k1) {
     uint32_t o[4];
     philox10(b, s0, s1, 0u, k0, k1, o);
     return make_uint4(o[0], o[1], o[2], o[3]);

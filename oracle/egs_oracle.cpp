@@ -32,8 +32,10 @@
 //   - the XYZ geometry bit for bit, and the parallel-beam source and spectrum
 //     in distribution, against the reference's own egs++ classes compiled from
 //     its sources (oracle/egspp_ref.cpp, tests/test_egspp_reference.py);
-//   - the Klein-Nishina, Sauter and Bethe-Heitler samplers against their
-//     analytic distributions (tests/test_oracle_samplers.py).
+//   - the interaction samplers against their cross sections: Klein-Nishina,
+//     Sauter, Bethe-Heitler pair, Moller, Bhabha, bremsstrahlung, Heitler's
+//     annihilation in flight, and Rayleigh with the form factors of the raw
+//     pgs4form.dat (tests/test_oracle_samplers.py).
 //
 // Random numbers: either one RANMAR stream for the whole run (as the
 // reference does) or Philox-4x32-10 (Salmon et al., SC'11) with one stream
